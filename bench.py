@@ -1,0 +1,447 @@
+"""Benchmark of the portBLAS hot path on GB300 (one JSON line on rank 0).
+
+Default workload — the memory-bound set, fp32, at its full sizes:
+  * _gemv 'n' and 't' on an 8192 x 8192 column-major A (lda 8192, incx = incy
+    = 1, alpha 1, beta 0), A ~ U[-1, 1];
+  * _asum, _nrm2, _dot, _iamax, _iamin on n = 2^26 vectors ~ N(0, 1), with the
+    largest |x| planted at 8 random indices (ties exercise the first-index rule);
+  * extension::_reduction Add, inner (column sums) and outer (row sums), over a
+    16384 x 16384 matrix.
+One step = one pass over all of them.  `value` is the step's algorithmic bytes
+(portBLAS's benchmark counters: common/include/common/blas{1,2}_state_counters.hpp)
+divided by the device time of the step, inputs resident in HBM; every input is
+larger than the 129 MB L2.  `e2e` is the same step through the public API with
+host buffers: pinned host->device copies of the inputs and device->host reads of
+the results are inside its timed region.  The SGEMM precision/throughput set
+(8192^3 NN and TN, entries s*2^u, u ~ U[-10, 10]: plain FP32 SIMT vs split-BF16
+on the tensor cores, errors against the FP64 oracle on sampled entries) and
+DGEMM 4096^3 are measured in the same run and reported under "sgemm".
+
+--impl reference times the reference's CPU path for the same step on the host
+cores: the CBLAS that portBLAS's tests link (numpy's bundled OpenBLAS) for
+GEMV and the BLAS-1 reductions, and the OpenMP C restatement of portBLAS's
+Reduction kernel for extension::_reduction (no CBLAS counterpart).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "SGEMM TFLOP/s split-BF16 vs FP32 @rel err≤1e-6; GEMV/asum GB/s vs HBM peak"
+F32 = 4
+GEMV_N = 8192
+VEC_N = 1 << 26
+RED_N = 16384
+
+
+def algorithmic_bytes() -> dict:
+    """Bytes per op, as portBLAS's counters count them."""
+    gemv = (GEMV_N * GEMV_N + GEMV_N + GEMV_N) * F32  # A + x + y (beta = 0: y written only)
+    return {
+        "gemv_n": gemv, "gemv_t": gemv,
+        "asum": (VEC_N + 1) * F32, "nrm2": (VEC_N + 1) * F32, "dot": (2 * VEC_N + 1) * F32,
+        "iamax": (VEC_N + 1) * F32, "iamin": (VEC_N + 1) * F32,
+        "reduction_inner": (RED_N * RED_N + RED_N) * F32, "reduction_outer": (RED_N * RED_N + RED_N) * F32,
+    }
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "src": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
+
+
+# ------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------- GPU side --
+def make_inputs(torch, dev):
+    gen = torch.Generator(device=dev).manual_seed(20240917)
+    A = torch.rand(GEMV_N * GEMV_N, device=dev, generator=gen) * 2 - 1
+    xg = torch.rand(GEMV_N, device=dev, generator=gen) * 2 - 1
+    v = torch.randn(VEC_N, device=dev, generator=gen)
+    w = torch.randn(VEC_N, device=dev, generator=gen)
+    # plant the largest |x| at 8 random indices with random signs
+    idx = torch.randperm(VEC_N, device=dev, generator=gen)[:8]
+    big = 8.0 * v.abs().max()
+    signs = torch.where(torch.rand(8, device=dev, generator=gen) < 0.5, -1.0, 1.0)
+    v[idx] = big * signs
+    R = torch.rand(RED_N * RED_N, device=dev, generator=gen) * 2 - 1
+    return dict(A=A, xg=xg, v=v, w=w, R=R, planted=int(idx.min().item()))
+
+
+def run_step(blas, sb, inp, outs, events=None):
+    """One pass of the memory-bound set; `events` (optional) brackets each op."""
+    ops = [
+        ("gemv_n", lambda: blas._gemv(sb, "n", GEMV_N, GEMV_N, 1.0, inp["A"], GEMV_N, inp["xg"], 1, 0.0,
+                                      outs["yn"], 1)),
+        ("gemv_t", lambda: blas._gemv(sb, "t", GEMV_N, GEMV_N, 1.0, inp["A"], GEMV_N, inp["xg"], 1, 0.0,
+                                      outs["yt"], 1)),
+        ("asum", lambda: blas._asum(sb, VEC_N, inp["v"], 1, outs["s"][0:1])),
+        ("nrm2", lambda: blas._nrm2(sb, VEC_N, inp["v"], 1, outs["s"][1:2])),
+        ("dot", lambda: blas._dot(sb, VEC_N, inp["v"], 1, inp["w"], 1, outs["s"][2:3])),
+        ("iamax", lambda: blas._iamax(sb, VEC_N, inp["v"], 1, outs["i"][0:1])),
+        ("iamin", lambda: blas._iamin(sb, VEC_N, inp["v"], 1, outs["i"][1:2])),
+        ("reduction_inner", lambda: blas.extension._reduction(blas.AddOperator, sb, inp["R"], RED_N, outs["ri"],
+                                                              RED_N, RED_N, blas.reduction_dim_t.inner)),
+        ("reduction_outer", lambda: blas.extension._reduction(blas.AddOperator, sb, inp["R"], RED_N, outs["ro"],
+                                                              RED_N, RED_N, blas.reduction_dim_t.outer)),
+    ]
+    for i, (name, fn) in enumerate(ops):
+        if events is not None:
+            events[name][0].record()
+        fn()
+        if events is not None:
+            events[name][1].record()
+    return [n for n, _ in ops]
+
+
+def bench_memory_set(torch, blas, sb, steps, warmup, dev):
+    inp = make_inputs(torch, dev)
+    outs = dict(yn=torch.empty(GEMV_N, device=dev), yt=torch.empty(GEMV_N, device=dev),
+                s=torch.zeros(3, device=dev), i=torch.zeros(2, dtype=torch.int32, device=dev),
+                ri=torch.empty(RED_N, device=dev), ro=torch.empty(RED_N, device=dev))
+    names = list(algorithmic_bytes())
+    for _ in range(warmup):
+        run_step(blas, sb, inp, outs)
+    torch.cuda.synchronize()
+    # per-op device times (events around each op, separate pass)
+    per_op = {n: [] for n in names}
+    for _ in range(max(3, min(steps, 10))):
+        ev = {n: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for n in names}
+        run_step(blas, sb, inp, outs, ev)
+        torch.cuda.synchronize()
+        for n in names:
+            per_op[n].append(ev[n][0].elapsed_time(ev[n][1]))
+    # the timed region: K whole steps between two events
+    l0 = blas.launch_count()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        time.sleep(0.3)
+        start.record()
+        for _ in range(steps):
+            run_step(blas, sb, inp, outs)
+        end.record()
+        torch.cuda.synchronize()
+        time.sleep(0.2)
+    launches = blas.launch_count() - l0
+    ms = start.elapsed_time(end) / steps
+    # correctness spot checks of the last step
+    iam = outs["i"].cpu().numpy()
+    checks = {"iamax_index": int(iam[0]), "iamax_expected_first_planted": inp["planted"]}
+    return dict(ms=ms, per_op={n: statistics.median(v) for n, v in per_op.items()}, launches=launches,
+                clocks=clk.summary(), checks=checks, inp=inp, outs=outs)
+
+
+def bench_e2e(torch, blas, sb, steps, warmup, dev):
+    """Same step through the public API with host buffers: H2D of every input
+    (pinned) and D2H of every result inside the timed region."""
+    g = np.random.default_rng(7)
+    host = dict(
+        A=torch.from_numpy(g.uniform(-1, 1, GEMV_N * GEMV_N).astype(np.float32)).pin_memory(),
+        xg=torch.from_numpy(g.uniform(-1, 1, GEMV_N).astype(np.float32)).pin_memory(),
+        v=torch.from_numpy(g.standard_normal(VEC_N).astype(np.float32)).pin_memory(),
+        w=torch.from_numpy(g.standard_normal(VEC_N).astype(np.float32)).pin_memory(),
+        R=torch.from_numpy(g.uniform(-1, 1, RED_N * RED_N).astype(np.float32)).pin_memory(),
+    )
+    dev_in = {k: torch.empty_like(v, device=dev) for k, v in host.items()}
+    outs = dict(yn=torch.empty(GEMV_N, device=dev), yt=torch.empty(GEMV_N, device=dev),
+                s=torch.zeros(3, device=dev), i=torch.zeros(2, dtype=torch.int32, device=dev),
+                ri=torch.empty(RED_N, device=dev), ro=torch.empty(RED_N, device=dev))
+    host_out = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in outs.items()}
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    d2h = sum(v.numel() * v.element_size() for v in outs.values())
+
+    def step():
+        for k in host:
+            dev_in[k].copy_(host[k], non_blocking=True)
+        run_step(blas, sb, dev_in, outs)
+        for k in outs:
+            host_out[k].copy_(outs[k], non_blocking=True)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        step()
+    end.record()
+    torch.cuda.synchronize()
+    return dict(ms=start.elapsed_time(end) / steps, h2d=h2d, d2h=d2h)
+
+
+def bench_sgemm(torch, blas, sb, dev, reps=3):
+    """8192^3 FP32 GEMM: plain SIMT vs split-BF16 (x3 and x6 products), NN and TN,
+    entries s*2^u (u ~ U[-10, 10]); error vs the FP64 oracle on sampled entries."""
+    import oracle
+    n = 8192
+    g = np.random.default_rng(99)
+
+    def pw2(size):
+        u = g.uniform(-10, 10, size)
+        s = g.choice([-1.0, 1.0], size)
+        return (s * np.exp2(u)).astype(np.float32)
+
+    a = pw2(n * n)
+    b = pw2(n * n)
+    ad, bd = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    cd = torch.zeros(n * n, device=dev)
+    rows = g.integers(0, n, 256)
+    cols = g.integers(0, n, 256)
+    res = {}
+    modes = [("fp32_simt", blas.sgemm_mode_t.fp32_simt), ("split_bf16x3", blas.sgemm_mode_t.split_bf16x3),
+             ("split_bf16x6", blas.sgemm_mode_t.split_bf16x6)]
+    for ta in (False, True):
+        tag = "TN" if ta else "NN"
+        ref = oracle.gemm(ta, False, n, n, n, 1.0, a, n, b, n, 0.0, None, n, rows=rows, cols=cols)
+        scale = oracle.gemm_absscale(ta, False, n, n, n, 1.0, a, n, b, n, 0.0, None, n, rows=rows, cols=cols)
+        for name, mode in modes:
+            sb.set_sgemm_mode(mode)
+            try:
+                blas._gemm(sb, "t" if ta else "n", "n", n, n, n, 1.0, ad, n, bd, n, 0.0, cd, n)
+            except (blas.UnsupportedException, NotImplementedError) as e:
+                res[f"{name}_{tag}"] = {"unavailable": str(e)}
+                continue
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                blas._gemm(sb, "t" if ta else "n", "n", n, n, n, 1.0, ad, n, bd, n, 0.0, cd, n)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            got = cd.view(n, n).T.cpu().numpy()[rows, cols].astype(np.float64)
+            err = np.abs(got - ref)
+            ms = min(ts)
+            res[f"{name}_{tag}"] = {
+                "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "ms": ms,
+                "max_rel_err": float(np.max(err / np.maximum(np.abs(ref), 1e-300))),
+                "mean_rel_err": float(np.mean(err / np.maximum(np.abs(ref), 1e-300))),
+                "max_norm_err": float(np.max(err / scale)), "mean_norm_err": float(np.mean(err / scale)),
+                "sampled_entries": len(rows)}
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    # DGEMM 4096^3 on the FP64 pipe
+    nd = 4096
+    A = torch.rand(nd * nd, device=dev, dtype=torch.float64) * 2 - 1
+    B = torch.rand(nd * nd, device=dev, dtype=torch.float64) * 2 - 1
+    Cc = torch.zeros(nd * nd, device=dev, dtype=torch.float64)
+    blas._gemm(sb, "n", "n", nd, nd, nd, 1.0, A, nd, B, nd, 0.0, Cc, nd)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    blas._gemm(sb, "n", "n", nd, nd, nd, 1.0, A, nd, B, nd, 0.0, Cc, nd)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ref = (A.view(nd, nd).T[:64] @ B.view(nd, nd).T[:, :64])
+    derr = float(((Cc.view(nd, nd).T[:64, :64] - ref).abs().max() / ref.abs().max()).item())
+    res["dgemm_4096"] = {"tflops": 2.0 * nd ** 3 / (ms * 1e-3) / 1e12, "ms": ms, "max_err_vs_torch_fp64": derr}
+    del ad, bd, cd, A, B, Cc
+    torch.cuda.empty_cache()
+    simt = res.get("fp32_simt_NN", {}).get("tflops")
+    for k in ("split_bf16x3_NN", "split_bf16x6_NN"):
+        if simt and "tflops" in res.get(k, {}):
+            res[k]["speedup_vs_fp32_simt"] = res[k]["tflops"] / simt
+    return res
+
+
+# ----------------------------------------------------------- CPU side --
+def cpu_reference_step(cb, oracle_mod, data, outs):
+    """The memory-bound step on the host cores: OpenBLAS CBLAS + OpenMP C
+    restatement of the Reduction kernel."""
+    cb.sgemv("n", GEMV_N, GEMV_N, 1.0, data["A"], GEMV_N, data["xg"], 1, 0.0, outs["yn"], 1)
+    cb.sgemv("t", GEMV_N, GEMV_N, 1.0, data["A"], GEMV_N, data["xg"], 1, 0.0, outs["yt"], 1)
+    cb.sasum(VEC_N, data["v"], 1)
+    cb.snrm2(VEC_N, data["v"], 1)
+    cb.sdot(VEC_N, data["v"], 1, data["w"], 1)
+    cb.isamax(VEC_N, data["v"], 1)
+    np.argmin(np.abs(data["v"]))  # iamin has no CBLAS symbol: first strict minimum
+    oracle_mod.reduction("add", "inner", data["R64"], RED_N, RED_N, RED_N)
+    oracle_mod.reduction("add", "outer", data["R64"], RED_N, RED_N, RED_N)
+
+
+def cpu_reference_data():
+    g = np.random.default_rng(3)
+    R = g.uniform(-1, 1, RED_N * RED_N).astype(np.float32)
+    return dict(A=g.uniform(-1, 1, GEMV_N * GEMV_N).astype(np.float32),
+                xg=g.uniform(-1, 1, GEMV_N).astype(np.float32),
+                v=g.standard_normal(VEC_N).astype(np.float32), w=g.standard_normal(VEC_N).astype(np.float32),
+                R64=R.astype(np.float64))
+
+
+def bench_cpu(steps: int, warmup: int, budget_s: float = 20.0) -> dict:
+    import oracle
+    cores = os.cpu_count() or 1
+    cb = oracle.CBlas()
+    cb.set_threads(cores)
+    data = cpu_reference_data()
+    outs = dict(yn=np.empty(GEMV_N, np.float32), yt=np.empty(GEMV_N, np.float32))
+    for _ in range(max(1, warmup)):
+        cpu_reference_step(cb, oracle, data, outs)
+    ts = []
+    t_start = time.perf_counter()
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        cpu_reference_step(cb, oracle, data, outs)
+        ts.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    ms = statistics.median(ts) * 1e3
+    total = sum(algorithmic_bytes().values())
+    return dict(value=total / (ms * 1e-3) / 1e9, ms=ms, cores=cores, threads_oracle=oracle.num_threads(),
+                steps=len(ts))
+
+
+# --------------------------------------------------------------- main --
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
+    ap.add_argument("--no-sgemm", action="store_true", help="skip the SGEMM/DGEMM set")
+    args = ap.parse_args()
+    warmup = max(3, args.warmup)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    total_bytes = sum(algorithmic_bytes().values())
+    config = {"workload": "memory-bound set fp32: gemv N+T 8192^2, asum/nrm2/dot/iamax/iamin n=2^26, "
+                          "reduction Add inner+outer 16384^2",
+              "gemv": [GEMV_N, GEMV_N], "vector_n": VEC_N, "reduction": [RED_N, RED_N],
+              "bytes_per_step": total_bytes, "l2": "every input larger than L2 (no flush needed)",
+              "parallelism": f"replicas{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = bench_cpu(args.steps, args.warmup)
+        line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "GB/s", "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": config,
+                "cpu_baseline": {"value": r["value"], "unit": "GB/s", "cores": r["cores"], "kind": "port",
+                                 "sample": "full memory-bound step on the host: numpy-bundled OpenBLAS CBLAS "
+                                           "(sgemv N/T, sasum, snrm2, sdot, isamax; iamin by first strict minimum) "
+                                           "+ OpenMP C restatement of portBLAS Reduction (FP64 accumulate)"},
+                "e2e": {"value": r["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    import __graft_entry__
+    __graft_entry__.build()
+    from portblas_gb300 import blas
+    sb = blas.SB_Handle()
+    mem = bench_memory_set(torch, blas, sb, args.steps, warmup, dev)
+    e2e = bench_e2e(torch, blas, sb, max(3, args.steps // 4), 3, dev)
+    ms = mem["ms"]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms, e2e["ms"]], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    else:
+        e2e_ms = e2e["ms"]
+    value = world * total_bytes / (ms * 1e-3) / 1e9
+    pk = peaks()
+    ab = algorithmic_bytes()
+    dom = max(mem["per_op"], key=lambda n: mem["per_op"][n])
+    achieved = ab[dom] / (mem["per_op"][dom] * 1e-3) / 1e9
+    sg = None
+    if not args.no_sgemm:
+        sg = bench_sgemm(torch, blas, sb, dev)
+    if rank != 0:
+        return
+    cpu = bench_cpu(2, 1, budget_s=15.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)", "config": config,
+        "hbm_frac_of_" + pk["src"]: value / world / pk["hbm_gbs"],
+        "per_op": {n: {"ms": t, "gbs": ab[n] / (t * 1e-3) / 1e9, "frac": ab[n] / (t * 1e-3) / 1e9 / pk["hbm_gbs"]}
+                   for n, t in mem["per_op"].items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "peak_src": pk["src"], "traffic": None},
+        "e2e": {"value": world * total_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+                "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]},
+        "gpu_launches": mem["launches"], "clocks": mem["clocks"], "checks": mem["checks"],
+        "cpu_baseline": {"value": cpu["value"], "unit": "GB/s", "cores": cpu["cores"], "kind": "port",
+                         "sample": f"{cpu['steps']} full memory-bound steps on the host (OpenBLAS CBLAS + "
+                                   "OpenMP C Reduction restatement), median"},
+        "sgemm": sg,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

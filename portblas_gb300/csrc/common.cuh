@@ -1,0 +1,96 @@
+// common.cuh — shared host/device helpers of the gbblas library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <mutex>
+#include <string>
+
+#include "../../include/gbblas.h"
+
+namespace gb {
+
+// ----------------------------------------------------------------- errors --
+// Per-thread message of the last failing call (gbblas_last_error).
+void set_error(const std::string& msg);
+void clear_error();
+
+struct Status {
+  gbblas_status_t code = GBBLAS_STATUS_SUCCESS;
+};
+
+inline gbblas_status_t fail(gbblas_status_t code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+inline gbblas_status_t cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return GBBLAS_STATUS_CUDA_ERROR;
+}
+
+#define GB_CUDA_TRY(expr)                                   \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) return ::gb::cuda_fail(_e, #expr); \
+  } while (0)
+
+#define GB_TRY(expr)                                         \
+  do {                                                       \
+    gbblas_status_t _s = (expr);                             \
+    if (_s != GBBLAS_STATUS_SUCCESS) return _s;              \
+  } while (0)
+
+// Checks the launch that was just issued and counts it.
+gbblas_status_t after_launch(const char* kernel);
+
+// ----------------------------------------------------------------- handle --
+}  // namespace gb
+
+struct gbblas_handle_s {
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int sm_count = 0;
+  int max_smem_optin = 0;
+  // Stream-ordered temp memory: one growable block, released with
+  // cudaFreeAsync on the same stream (the portBLAS Temp_Mem_Pool equivalent,
+  // include/sb_handle/temp_memory_pool.h:33-114).
+  void* temp = nullptr;
+  size_t temp_size = 0;
+  // Zero-initialised ticket counters used by the last-block-done reductions.
+  // Every kernel that takes tickets resets the ones it used before exiting.
+  unsigned int* tickets = nullptr;
+  size_t n_tickets = 0;
+  // Device error word written by bounded waits that gave up.
+  int* dev_error = nullptr;
+  // Pinned host staging for the *_sync overloads.
+  void* pinned = nullptr;
+  int sgemm_mode = GBBLAS_SGEMM_AUTO;
+  std::mutex mu;  // guards temp memory, as the portBLAS pool mutex does
+};
+
+namespace gb {
+
+// Returns a device pointer to at least `bytes` of temp memory, 256-byte aligned.
+// Stream-ordered: the block stays valid for everything enqueued afterwards on
+// the handle's stream until the next call that grows it.
+gbblas_status_t temp_acquire(gbblas_handle_t h, size_t bytes, void** ptr);
+// Number of ticket counters available: kMaxTickets.
+constexpr size_t kMaxTickets = 1u << 16;
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Element i of a strided vector view (portBLAS VectorView, src/views/view.hpp:43-48).
+template <typename T>
+__host__ __device__ __forceinline__ const T* vec_base(const T* x, int64_t n, int64_t inc) {
+  return inc >= 0 ? x : x + (n - 1) * (-inc);
+}
+template <typename T>
+__host__ __device__ __forceinline__ T* vec_base(T* x, int64_t n, int64_t inc) {
+  return inc >= 0 ? x : x + (n - 1) * (-inc);
+}
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace gb

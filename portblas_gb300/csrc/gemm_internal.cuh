@@ -1,0 +1,42 @@
+// gemm_internal.cuh — internal launch interface of the GEMM kernels.
+#pragma once
+#include "common.cuh"
+
+namespace gb {
+
+// One (possibly batched) column-major GEMM problem.  Element (i, j) of op(A)
+// is A[i + j*lda] (ta false) or A[j + i*lda] (ta true); same for B.
+template <typename T>
+struct GemmArgs {
+  bool ta, tb;
+  int64_t m, n, k;
+  T alpha, beta;
+  const T* a;
+  int64_t lda, stride_a;
+  const T* b;
+  int64_t ldb, stride_b;
+  T* c;
+  int64_t ldc, stride_c;
+  int64_t batch;
+};
+
+// Plain FP32 / FP64 SIMT GEMM (CUDA cores), any transposes, strided batch.
+gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<float>& g);
+gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<double>& g);
+
+// C <- beta*C over a strided batch of M x N matrices (beta == 0 writes zeros):
+// the alpha == 0 path of gemm_interface.hpp:112-139.
+gbblas_status_t launch_scale_c(gbblas_handle_t h, int64_t m, int64_t n, float beta, float* c, int64_t ldc,
+                               int64_t stride_c, int64_t batch);
+gbblas_status_t launch_scale_c(gbblas_handle_t h, int64_t m, int64_t n, double beta, double* c, int64_t ldc,
+                               int64_t stride_c, int64_t batch);
+
+// Split-BF16 FP32 GEMM on the tcgen05 tensor cores (pieces = 2 or 3 BF16
+// terms per operand).  Returns UNSUPPORTED when the shape is not handled.
+gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces);
+
+// Method dispatch after argument checks (gemm.cu).
+gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g);
+gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<double>& g);
+
+}  // namespace gb

@@ -1,0 +1,107 @@
+// gemv.cu — y <- alpha*op(A)*x + beta*y on sm_103a.
+//
+// Replaces portBLAS's two-kernel GEMV (partial dot products into temp
+// memory, then SumMatrixColumns + ScalarOp/Assign:
+// src/interface/blas2_interface.hpp:68-217, src/operations/blas2/gemv.hpp:40-371)
+// with one HBM-bound sweep whose split partials are folded by the last CTA of
+// each output tile; the alpha/beta epilogue is fused.  beta == 0 never reads
+// y (blas2_interface.hpp:205-211); trans 'n'/'N' is the normal sweep and any
+// other character the transposed one (blas2_interface.hpp:1163-1192).
+#include "matvec.cuh"
+
+namespace gb {
+
+template <typename T>
+struct GemvPolicy {
+  using Acc = T;
+  T alpha, beta;
+  T* yb;  // base of the y view
+  int64_t incy;
+  __device__ __forceinline__ Acc init() const { return T(0); }
+  __device__ __forceinline__ void add(Acc& a, T v, T x) const { a = fma(v, x, a); }
+  __device__ __forceinline__ void merge(Acc& a, const Acc& b) const { a += b; }
+  __device__ __forceinline__ Acc shfl_down(const Acc& a, int off) const { return __shfl_down_sync(0xffffffffu, a, off); }
+  __device__ __forceinline__ void finish(const Acc& a, int64_t i) const {
+    T* yp = yb + i * incy;
+    T r = alpha * a;
+    if (beta != T(0)) r = fma(beta, *yp, r);
+    *yp = r;
+  }
+};
+
+template <typename T>
+gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T alpha, const T* a, int64_t lda,
+                          const T* x, int64_t incx, T beta, T* y, int64_t incy) {
+  if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "gemv: null handle");
+  if (m < 0 || n < 0) return fail(GBBLAS_STATUS_INVALID_ARG, "gemv: negative dimension");
+  if (incx == 0 || incy == 0) return fail(GBBLAS_STATUS_INVALID_ARG, "gemv: zero increment");
+  if (lda < 0) return fail(GBBLAS_STATUS_INVALID_ARG, "gemv: negative lda");
+  const bool tr = !(trans == 'n' || trans == 'N');
+  const int64_t xlen = tr ? m : n, ylen = tr ? n : m;
+  if (ylen == 0) return GBBLAS_STATUS_SUCCESS;
+  if (!y || (xlen > 0 && (!a || !x))) return fail(GBBLAS_STATUS_INVALID_ARG, "gemv: null pointer");
+  GemvPolicy<T> pol{alpha, beta, vec_base(y, ylen, incy), incy};
+  const T* xb = vec_base(x, xlen, incx);
+  constexpr int RPT = 16 / sizeof(T);
+  const bool vec = (lda % RPT == 0) && aligned16(a);
+  if (!tr) {
+    SweepPlan p = plan_rows(m, n, h->sm_count, sizeof(T));
+    T* partials = nullptr;
+    if (p.split > 1) {
+      void* tmp;
+      GB_TRY(temp_acquire(h, sizeof(T) * p.split * m, &tmp));
+      partials = static_cast<T*>(tmp);
+    }
+    dim3 grid(unsigned(p.tiles), unsigned(p.split));
+    if (vec)
+      rows_sweep<GemvPolicy<T>, T, true, true><<<grid, kMvThreads, 0, h->stream>>>(
+          pol, m, n, a, lda, xb, incx, p.per_split, partials, h->tickets);
+    else
+      rows_sweep<GemvPolicy<T>, T, false, true><<<grid, kMvThreads, 0, h->stream>>>(
+          pol, m, n, a, lda, xb, incx, p.per_split, partials, h->tickets);
+    return after_launch("gemv_n");
+  }
+  SweepPlan p = plan_cols(m, n, h->sm_count, sizeof(T));
+  const int64_t chunk_cols = int64_t(kMaxTickets) * p.cols_per_cta;
+  T* partials = nullptr;
+  if (p.split > 1) {
+    void* tmp;
+    GB_TRY(temp_acquire(h, sizeof(T) * p.split * (n < chunk_cols ? n : chunk_cols), &tmp));
+    partials = static_cast<T*>(tmp);
+  }
+  const size_t smem = ((p.per_split * sizeof(T) + 15) & ~size_t(15)) + sizeof(T) * p.cols_per_cta;
+  for (int64_t c0 = 0; c0 < n; c0 += chunk_cols) {
+    const int64_t nc = n - c0 < chunk_cols ? n - c0 : chunk_cols;
+    GemvPolicy<T> pc = pol;
+    pc.yb = pol.yb + c0 * incy;
+    dim3 grid(unsigned(cdiv(nc, p.cols_per_cta)), unsigned(p.split));
+    if (vec)
+      cols_sweep<GemvPolicy<T>, T, true, true><<<grid, kMvThreads, smem, h->stream>>>(
+          pc, m, nc, a + c0 * lda, lda, xb, incx, p.per_split, p.cols_per_cta, partials, h->tickets);
+    else
+      cols_sweep<GemvPolicy<T>, T, false, true><<<grid, kMvThreads, smem, h->stream>>>(
+          pc, m, nc, a + c0 * lda, lda, xb, incx, p.per_split, p.cols_per_cta, partials, h->tickets);
+    GB_TRY(after_launch("gemv_t"));
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+gbblas_status_t gbblas_sgemv(gbblas_handle_t h, char trans, int64_t m, int64_t n, float alpha, const float* a,
+                             int64_t lda, const float* x, int64_t incx, float beta, float* y, int64_t incy) {
+  clear_error();
+  return gemv_impl<float>(h, trans, m, n, alpha, a, lda, x, incx, beta, y, incy);
+}
+
+gbblas_status_t gbblas_dgemv(gbblas_handle_t h, char trans, int64_t m, int64_t n, double alpha, const double* a,
+                             int64_t lda, const double* x, int64_t incx, double beta, double* y, int64_t incy) {
+  clear_error();
+  return gemv_impl<double>(h, trans, m, n, alpha, a, lda, x, incx, beta, y, incy);
+}
+
+}  // extern "C"

@@ -1,0 +1,254 @@
+// matvec.cuh — the two HBM-bound column-major matrix sweeps shared by GEMV
+// and extension::_reduction.
+//
+//   rows sweep  (GEMV 'n', reduction outer): out(i) = fold_j  f(A(i,j), x_j)
+//   cols sweep  (GEMV 't', reduction inner): out(j) = fold_i  f(A(i,j), x_i)
+//
+// Both read A exactly once with 128-bit coalesced loads (when lda and the
+// base allow it), keep several loads in flight per thread, and split the
+// folded dimension across CTAs when the preserved dimension alone cannot
+// fill the 152 SMs.  Split partials go to temp memory; the last CTA of each
+// output tile (a per-tile ticket, no waiting) folds them in split order and
+// runs the epilogue, so results are deterministic.
+//
+// Policy supplies: Acc, init(), add(acc, a, x), merge(acc, other),
+// finish(acc, out_index) -> writes the output element.
+#pragma once
+
+#include "common.cuh"
+#include "reduce_util.cuh"
+
+namespace gb {
+
+template <typename T>
+struct Pack16;
+template <>
+struct Pack16<float> {
+  using V = float4;
+  static constexpr int n = 4;
+  __device__ static void get(const V& v, float* o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+};
+template <>
+struct Pack16<double> {
+  using V = double2;
+  static constexpr int n = 2;
+  __device__ static void get(const V& v, double* o) { o[0] = v.x; o[1] = v.y; }
+};
+
+constexpr int kMvThreads = 256;
+constexpr int kMvWarps = kMvThreads / 32;
+
+// ------------------------------------------------------------- rows sweep --
+// CTA = 8 warps over a block of 32*RPT rows; warp w takes columns
+// c0+w, c0+w+8, ... of its split; the 8 warp partials fold in warp order.
+template <class P, typename T, bool VEC, bool HAS_X>
+__global__ void __launch_bounds__(kMvThreads)
+    rows_sweep(P pol, int64_t M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
+               int64_t incx, int64_t cols_per_split, typename P::Acc* __restrict__ partials,
+               unsigned int* __restrict__ tickets) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  constexpr int WR = 32 * RPT;
+  __shared__ Acc red[kMvWarps][WR];
+  __shared__ bool is_last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rblock = blockIdx.x;
+  const int64_t row0 = rblock * WR + lane * RPT;
+  const int64_t c0 = int64_t(blockIdx.y) * cols_per_split;
+  const int64_t c1 = min(N, c0 + cols_per_split);
+  Acc acc[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
+  const bool full = VEC && (row0 + RPT <= M);
+  const T* Ap = A + row0;
+
+  auto load_col = [&](int64_t j, T* v) {
+    if (full) {
+      Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(Ap + j * lda)), v);
+    } else {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) v[r] = (row0 + r < M) ? Ap[j * lda + r] : T(0);
+    }
+  };
+
+  int64_t j = c0 + warp;
+  constexpr int U = 4;
+  for (; j + (U - 1) * kMvWarps < c1; j += U * kMvWarps) {
+    T v[U][RPT];
+    T xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      load_col(j + u * kMvWarps, v[u]);
+      xv[u] = HAS_X ? xb[(j + u * kMvWarps) * incx] : T(1);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[u][r], xv[u]);
+  }
+  for (; j < c1; j += kMvWarps) {
+    T v[RPT];
+    load_col(j, v);
+    T xv = HAS_X ? xb[j * incx] : T(1);
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[r], xv);
+  }
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) red[warp][lane * RPT + r] = acc[r];
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int64_t row = rblock * WR + t;
+  Acc s;
+  if (t < WR) {
+    s = red[0][t];
+#pragma unroll
+    for (int w = 1; w < kMvWarps; ++w) pol.merge(s, red[w][t]);
+  }
+  if (gridDim.y == 1) {
+    if (t < WR && row < M) pol.finish(s, row);
+    return;
+  }
+  if (t < WR && row < M) partials[int64_t(blockIdx.y) * M + row] = s;
+  __threadfence();
+  __syncthreads();
+  if (t == 0) is_last = atomicAdd(tickets + rblock, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (t < WR && row < M) {
+    Acc f = ldcg_any(partials + row);
+    for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * M + row));
+    pol.finish(f, row);
+  }
+  if (t == 0) tickets[rblock] = 0u;
+}
+
+// ------------------------------------------------------------- cols sweep --
+// CTA = 8 warps over CC columns and one chunk of `rows_per_split` rows; x of
+// the chunk is staged in shared memory; warp w takes columns w, w+8, ... and
+// reads each column chunk with 128-bit loads, 4 in flight per lane.
+template <class P, typename T, bool VEC, bool HAS_X>
+__global__ void __launch_bounds__(kMvThreads)
+    cols_sweep(P pol, int64_t M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
+               int64_t incx, int64_t rows_per_split, int cols_per_cta, typename P::Acc* __restrict__ partials,
+               unsigned int* __restrict__ tickets) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  constexpr int WR = 32 * RPT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* xs = reinterpret_cast<T*>(smem_raw);
+  Acc* colres = reinterpret_cast<Acc*>(smem_raw + ((rows_per_split * sizeof(T) + 15) & ~size_t(15)));
+  __shared__ bool is_last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r0 = int64_t(blockIdx.y) * rows_per_split;
+  const int64_t rlen = min(M - r0, rows_per_split);
+  if (HAS_X)
+    for (int64_t t = threadIdx.x; t < rows_per_split; t += blockDim.x) xs[t] = t < rlen ? xb[(r0 + t) * incx] : T(0);
+  __syncthreads();
+  const int64_t cbase = int64_t(blockIdx.x) * cols_per_cta;
+  for (int cc = warp; cc < cols_per_cta; cc += kMvWarps) {
+    const int64_t jcol = cbase + cc;
+    if (jcol >= N) break;
+    const T* col = A + jcol * lda + r0;
+    constexpr int U = 4;
+    Acc acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc[u] = pol.init();
+    int64_t r = int64_t(lane) * RPT;
+    if (VEC) {
+      for (; r + (U - 1) * WR + RPT <= rlen; r += U * WR) {
+        T v[U][RPT];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(col + r + u * WR)), v[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int e = 0; e < RPT; ++e) pol.add(acc[u], v[u][e], HAS_X ? xs[r + u * WR + e] : T(1));
+      }
+    }
+    for (; r < rlen; r += WR) {
+#pragma unroll
+      for (int e = 0; e < RPT; ++e)
+        if (r + e < rlen) pol.add(acc[0], col[r + e], HAS_X ? xs[r + e] : T(1));
+    }
+#pragma unroll
+    for (int u = 1; u < U; ++u) pol.merge(acc[0], acc[u]);
+    Acc s = acc[0];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) pol.merge(s, pol.shfl_down(s, off));
+    if (lane == 0) {
+      if (gridDim.y == 1) pol.finish(s, jcol);
+      else colres[cc] = s;
+    }
+  }
+  if (gridDim.y == 1) return;
+  __syncthreads();
+  for (int cc = threadIdx.x; cc < cols_per_cta; cc += blockDim.x) {
+    const int64_t jcol = cbase + cc;
+    if (jcol < N) partials[int64_t(blockIdx.y) * N + jcol] = colres[cc];
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(tickets + blockIdx.x, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int cc = threadIdx.x; cc < cols_per_cta; cc += blockDim.x) {
+    const int64_t jcol = cbase + cc;
+    if (jcol >= N) break;
+    Acc f = ldcg_any(partials + jcol);
+    for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + jcol));
+    pol.finish(f, jcol);
+  }
+  if (threadIdx.x == 0) tickets[blockIdx.x] = 0u;
+}
+
+// ------------------------------------------------------------------- host --
+struct SweepPlan {
+  int64_t split;      // number of CTAs along the folded dimension
+  int64_t per_split;  // folded elements per split
+  int cols_per_cta;   // cols sweep only
+  int64_t tiles;      // CTAs along the preserved dimension
+};
+
+// rows sweep: preserved = M (rows), folded = N (cols)
+inline SweepPlan plan_rows(int64_t M, int64_t N, int sm_count, int elem_bytes) {
+  const int64_t WR = 32 * (16 / elem_bytes);
+  SweepPlan p;
+  p.tiles = cdiv(M > 0 ? M : 1, WR);
+  const int64_t target = int64_t(sm_count) * 8;
+  int64_t split = cdiv(target, p.tiles);
+  const int64_t max_split = cdiv(N > 0 ? N : 1, 64);
+  if (split > max_split) split = max_split;
+  if (split < 1) split = 1;
+  if (p.tiles > int64_t(kMaxTickets)) split = 1;
+  p.per_split = split > 1 ? cdiv(N, split) : N;
+  p.split = split > 1 ? cdiv(N, p.per_split) : 1;
+  p.cols_per_cta = 0;
+  return p;
+}
+
+// cols sweep: preserved = N (cols), folded = M (rows)
+inline SweepPlan plan_cols(int64_t M, int64_t N, int sm_count, int elem_bytes) {
+  const int64_t WR = 32 * (16 / elem_bytes);
+  SweepPlan p;
+  p.cols_per_cta = 32;
+  if (N < 8 * int64_t(sm_count)) p.cols_per_cta = 8;
+  p.tiles = cdiv(N > 0 ? N : 1, p.cols_per_cta);
+  const int64_t target = int64_t(sm_count) * 8;
+  int64_t split = cdiv(target, p.tiles);
+  const int64_t max_rows = 4096;  // shared-memory x chunk bound
+  const int64_t min_split = cdiv(M > 0 ? M : 1, max_rows);
+  const int64_t max_split = cdiv(M > 0 ? M : 1, 4 * WR);
+  if (split > max_split) split = max_split;
+  if (split < min_split) split = min_split;
+  if (split < 1) split = 1;
+  int64_t per = cdiv(M > 0 ? M : 1, split);
+  per = cdiv(per, WR) * WR;
+  p.per_split = per;
+  p.split = cdiv(M > 0 ? M : 1, per);
+  return p;
+}
+
+}  // namespace gb

@@ -1,0 +1,183 @@
+"""GPU parity of _gemm / _gemm_batched / _gemm_strided_batched against the
+oracle through the C ABI, on portBLAS's sweep
+(test/unittest/blas3/blas3_gemm_test.cpp:29-141, blas3_gemm_batched_test.cpp,
+verify_gemm in blas3_gemm_common.hpp:96-230), for each FP32 method."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.util import rng, to_dev, to_host, assert_almost_equal
+
+pytestmark = pytest.mark.gpu
+KAT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "kat.json")))
+MODES = ["fp32_simt"]
+
+
+def _mats(g, ta, tb, m, n, k, lda_mul, ldb_mul, ldc_mul, off, dtype):
+    lda = (k if ta else m) * lda_mul
+    ldb = (n if tb else k) * ldb_mul
+    ldc = m * ldc_mul
+    a = g.uniform(-2, 5, off + lda * (m if ta else k)).astype(dtype)
+    b = g.uniform(-2, 5, off + ldb * (k if tb else n)).astype(dtype)
+    c = g.uniform(-2, 5, off + ldc * n).astype(dtype)
+    return a, lda, b, ldb, c, ldc
+
+
+def _gemm(sb, torch, mode, ta, tb, m, n, k, alpha, beta, lda_mul=1, ldb_mul=1, ldc_mul=1, off=0,
+          dtype=np.float32, seed=0, c_nan=False):
+    from portblas_gb300 import blas
+    g = rng(seed + m * 3 + n * 5 + k * 7)
+    a, lda, b, ldb, c, ldc = _mats(g, ta, tb, m, n, k, lda_mul, ldb_mul, ldc_mul, off, dtype)
+    if c_nan:
+        c[:] = np.nan
+    ref = oracle.gemm(ta, tb, m, n, k, alpha, a[off:], lda, b[off:], ldb, beta, c[off:], ldc)
+    if mode is not None:
+        sb.set_sgemm_mode(getattr(blas.sgemm_mode_t, mode))
+    ad, bd, cd = to_dev(a, torch), to_dev(b, torch), to_dev(c, torch)
+    blas._gemm(sb, "t" if ta else "n", "t" if tb else "n", m, n, k, alpha, ad[off:], lda, bd[off:], ldb, beta,
+               cd[off:], ldc)
+    out = to_host(cd)
+    got = out[off:off + ldc * n].reshape(n, ldc).T[:m]
+    # bytes outside the m x n window must be untouched
+    full = c.copy()
+    win = full[off:off + ldc * n].reshape(n, ldc).T
+    win[:m] = got
+    np.testing.assert_array_equal(np.isnan(out), np.isnan(full))
+    np.testing.assert_array_equal(np.nan_to_num(out), np.nan_to_num(full))
+    return got, ref
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("m,n,k", [(11, 11, 16), (16, 63, 17), (63, 16, 63), (253, 32, 253), (32, 253, 511),
+                                   (129, 257, 64)])
+@pytest.mark.parametrize("alpha,beta", [(1.5, 0.0), (1.0, 1.0), (1.5, 1.5), (0.0, 1.5)])
+def test_gemm_sweep(sb, torch_cuda, mode, ta, tb, m, n, k, alpha, beta):
+    got, ref = _gemm(sb, torch_cuda, mode, ta, tb, m, n, k, alpha, beta)
+    assert_almost_equal(got, ref)
+    np.testing.assert_allclose(got, ref, rtol=1e-5 * np.sqrt(k), atol=1e-5 * np.sqrt(k) * 25 * k)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("lda_mul,ldb_mul,ldc_mul,off", [(2, 3, 4, 0), (1, 1, 1, 1), (3, 2, 1, 10)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, True)])
+def test_gemm_ld_and_offsets(sb, torch_cuda, mode, lda_mul, ldb_mul, ldc_mul, off, ta, tb):
+    got, ref = _gemm(sb, torch_cuda, mode, ta, tb, 63, 45, 37, 1.5, 0.5, lda_mul, ldb_mul, ldc_mul, off)
+    assert_almost_equal(got, ref)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("alpha", [1.0, 0.0])
+def test_gemm_beta0_never_reads_c(sb, torch_cuda, mode, alpha):
+    got, ref = _gemm(sb, torch_cuda, mode, False, False, 33, 17, 9, alpha, 0.0, c_nan=True)
+    assert np.all(np.isfinite(got))
+    assert_almost_equal(got, ref)
+
+
+@pytest.mark.parametrize("case", KAT["gemm"], ids=lambda c: f"{c['ta']}{c['tb']}-a{c['alpha']}-b{c['beta']}")
+def test_gemm_kat(sb, torch_cuda, case):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    c = np.array(case["c"], dtype=np.float32)
+    if case["c_nan"]:
+        c[:] = np.nan
+    cd = to_dev(c, torch)
+    blas._gemm(sb, case["ta"], case["tb"], case["m"], case["n"], case["k"], case["alpha"],
+               to_dev(np.array(case["a"], dtype=np.float32), torch), case["lda"],
+               to_dev(np.array(case["b"], dtype=np.float32), torch), case["ldb"], case["beta"], cd, case["ldc"])
+    np.testing.assert_array_equal(to_host(cd), np.array(case["expected"], dtype=np.float32))
+
+
+def test_gemm_invalid_trans_raises(sb, torch_cuda):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    x = torch.zeros(16, device="cuda")
+    with pytest.raises(blas.InvalidArgument, match="_TransA"):
+        blas._gemm(sb, "x", "n", 4, 4, 4, 1.0, x, 4, x, 4, 0.0, x, 4)
+    with pytest.raises(blas.InvalidArgument, match="_TransB"):
+        blas._gemm(sb, "n", "q", 4, 4, 4, 1.0, x, 4, x, 4, 0.0, x, 4)
+    # alpha == 0 skips trans validation (gemm_interface.hpp:112-139)
+    blas._gemm(sb, "x", "n", 4, 4, 4, 0.0, x, 4, x, 4, 0.0, x, 4)
+
+
+def test_gemm_strided_invalid_strides(sb, torch_cuda):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    x = torch.zeros(1024, device="cuda")
+    with pytest.raises(blas.InvalidArgument, match="_stridec"):
+        blas._gemm_strided_batched(sb, "n", "n", 4, 4, 4, 1.0, x, 4, 16, x, 4, 16, 0.0, x, 4, 15, 2)
+    with pytest.raises(blas.InvalidArgument, match="_stridea"):
+        blas._gemm_strided_batched(sb, "n", "n", 4, 4, 4, 1.0, x, 4, -1, x, 4, 16, 0.0, x, 4, 16, 2)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True)])
+@pytest.mark.parametrize("beta", [0.0, 1.5])
+def test_gemm_batched_default_strides(sb, torch_cuda, mode, ta, tb, beta):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(getattr(blas.sgemm_mode_t, mode))
+    g = rng(17)
+    m, n, k, batch = 37, 29, 23, 5
+    lda, ldb, ldc = (k if ta else m), (n if tb else k), m
+    sa, sbb, sc = (m * lda if ta else k * lda), (ldb * k if tb else n * ldb), ldc * n
+    a = g.uniform(-2, 5, sa * batch).astype(np.float32)
+    b = g.uniform(-2, 5, sbb * batch).astype(np.float32)
+    c = g.uniform(-2, 5, sc * batch).astype(np.float32)
+    cd = to_dev(c, torch)
+    blas._gemm_batched(sb, "t" if ta else "n", "t" if tb else "n", m, n, k, 1.5, to_dev(a, torch), lda,
+                       to_dev(b, torch), ldb, beta, cd, ldc, batch)
+    out = to_host(cd)
+    for i in range(batch):
+        ref = oracle.gemm(ta, tb, m, n, k, 1.5, a[i * sa:], lda, b[i * sbb:], ldb, beta, c[i * sc:], ldc)
+        assert_almost_equal(out[i * sc:(i + 1) * sc].reshape(n, ldc).T[:m], ref)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("stride_mul", [1, 2])
+def test_gemm_strided_batched(sb, torch_cuda, mode, stride_mul):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(getattr(blas.sgemm_mode_t, mode))
+    g = rng(19)
+    m, n, k, batch = 64, 64, 64, 7
+    sa, sbb, sc = m * k * stride_mul, 0, m * n * stride_mul  # stride_b == 0 shares B
+    a = g.uniform(-1, 1, sa * batch).astype(np.float32)
+    b = g.uniform(-1, 1, k * n).astype(np.float32)
+    c = g.uniform(-1, 1, sc * batch).astype(np.float32)
+    cd = to_dev(c, torch)
+    blas._gemm_strided_batched(sb, "n", "n", m, n, k, 1.0, to_dev(a, torch), m, sa, to_dev(b, torch), k, sbb, 0.5,
+                               cd, m, sc, batch)
+    out = to_host(cd)
+    for i in range(batch):
+        ref = oracle.gemm(False, False, m, n, k, 1.0, a[i * sa:], m, b, k, 0.5, c[i * sc:], m)
+        assert_almost_equal(out[i * sc:i * sc + m * n].reshape(n, m).T, ref)
+        if stride_mul > 1:  # gap between matrices untouched
+            np.testing.assert_array_equal(out[i * sc + m * n:(i + 1) * sc], c[i * sc + m * n:(i + 1) * sc])
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False)])
+def test_dgemm(sb, torch_cuda, ta, tb):
+    got, ref = _gemm(sb, torch_cuda, None, ta, tb, 129, 65, 257, 1.5, 0.5, dtype=np.float64)
+    assert_almost_equal(got, ref, dtype=np.float64)
+
+
+def test_dgemm_strided_batched(sb, torch_cuda):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(23)
+    m = n = k = 33
+    batch = 3
+    a = g.uniform(-1, 1, m * k * batch)
+    b = g.uniform(-1, 1, k * n * batch)
+    c = np.zeros(m * n * batch)
+    cd = to_dev(c, torch)
+    blas._gemm_strided_batched(sb, "n", "t", m, n, k, 1.0, to_dev(a, torch), m, m * k, to_dev(b, torch), n, k * n,
+                               0.0, cd, m, m * n, batch)
+    out = to_host(cd)
+    for i in range(batch):
+        ref = oracle.gemm(False, True, m, n, k, 1.0, a[i * m * k:], m, b[i * k * n:], n, 0.0, None, m)
+        assert_almost_equal(out[i * m * n:(i + 1) * m * n].reshape(n, m).T, ref, dtype=np.float64)

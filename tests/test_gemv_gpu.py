@@ -1,0 +1,78 @@
+"""GPU parity of _gemv against the oracle through the C ABI, on portBLAS's
+sweep (test/unittest/blas2/blas2_gemv_test.cpp:123-151) plus edge cases."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.util import rng, to_dev, to_host, assert_almost_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(sb, torch, trans, m, n, alpha, beta, incx, incy, lda_mul=1, dtype=np.float32, seed=0, y_nan=False):
+    from portblas_gb300 import blas
+    g = rng(seed + m + n)
+    lda = m * lda_mul
+    a = g.uniform(-2, 5, lda * n).astype(dtype)
+    xlen, ylen = (n, m) if trans in "nN" else (m, n)
+    x = g.uniform(-2, 5, xlen * abs(incx)).astype(dtype)
+    y = g.uniform(-2, 5, ylen * abs(incy)).astype(dtype)
+    if y_nan:
+        y[:] = np.nan
+    ref = oracle.gemv(trans, m, n, alpha, a, lda, x, incx, beta, y, incy)
+    yd = to_dev(y, torch)
+    blas._gemv(sb, trans, m, n, alpha, to_dev(a, torch), lda, to_dev(x, torch), incx, beta, yd, incy)
+    got = oracle.view(to_host(yd), ylen, incy)
+    return got, ref
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+@pytest.mark.parametrize("m,n", [(11, 14), (11, 1010), (1023, 14), (1023, 1010)])
+@pytest.mark.parametrize("beta", [0.0, 1.5])
+@pytest.mark.parametrize("incx,incy,lda_mul", [(2, 3, 2), (1, 1, 1), (-1, 2, 1)])
+def test_gemv_sweep(sb, torch_cuda, trans, m, n, beta, incx, incy, lda_mul):
+    got, ref = _run(sb, torch_cuda, trans, m, n, 1.5, beta, incx, incy, lda_mul)
+    assert_almost_equal(got, ref)
+    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=2e-5 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+def test_gemv_beta0_ignores_nan_y(sb, torch_cuda, trans):
+    got, ref = _run(sb, torch_cuda, trans, 37, 29, 1.0, 0.0, 1, 1, y_nan=True)
+    assert np.all(np.isfinite(got))
+    assert_almost_equal(got, ref)
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+@pytest.mark.parametrize("m,n", [(1, 1), (1, 3000), (3000, 1), (5, 0), (0, 5), (257, 131)])
+def test_gemv_edges(sb, torch_cuda, trans, m, n):
+    got, ref = _run(sb, torch_cuda, trans, m, n, 0.75, 0.25, 1, 1)
+    assert_almost_equal(got, ref)
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+def test_gemv_double(sb, torch_cuda, trans):
+    got, ref = _run(sb, torch_cuda, trans, 513, 257, 1.5, 0.5, 1, 2, dtype=np.float64)
+    assert_almost_equal(got, ref, dtype=np.float64)
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+def test_gemv_full_size_linearity(sb, torch_cuda, trans):
+    """8192 x 8192 (the benchmark size): y(A, x1 + x2) == y(A, x1) + y(A, x2)
+    to FP32 rounding, and a sampled row set against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    m = n = 8192
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    a = torch.rand(m * n, device="cuda", generator=gen) * 2 - 1
+    x1 = torch.rand(8192, device="cuda", generator=gen) * 2 - 1
+    x2 = torch.rand(8192, device="cuda", generator=gen) * 2 - 1
+    ys = [torch.empty(8192, device="cuda") for _ in range(3)]
+    for y, x in zip(ys, (x1, x2, x1 + x2)):
+        blas._gemv(sb, trans, m, n, 1.0, a, m, x, 1, 0.0, y, 1)
+    lin = (ys[0] + ys[1] - ys[2]).abs().max().item()
+    assert lin <= 1e-3
+    A = a.view(n, m).T.double()
+    ref = (A @ x1.double()) if trans == "n" else (A.T @ x1.double())
+    err = (ys[0].double() - ref).abs().max().item()
+    assert err <= 2e-5 * ref.abs().max().item() * 8
