@@ -1,13 +1,329 @@
-// gemm_tc.cu — split-BF16 FP32 GEMM on the tcgen05 tensor cores.
+// gemm_tc.cu — FP32 GEMM as split-BF16 products on the tcgen05 tensor cores.
+//
+// Each FP32 operand is split into P BF16 terms, x = x0 + x1 (+ x2), with
+// x_{i+1} = bf16(x - x0 - ... - x_i) (exact residuals in FP32).  The product
+// keeps the terms whose order is at least 2^-16 (P = 2: x0y0, x0y1, x1y0) or
+// 2^-24 (P = 3: the six terms with i + j <= 2); every BF16 x BF16 product is
+// exact and all of them accumulate in one FP32 accumulator in tensor memory.
+//
+// Pipeline per CTA (128 x BN output tile, BK = 64):
+//   warp 0      TMA producer: the P A-term tiles and P B-term tiles of one
+//               k-block per stage (128-byte swizzle, K-major);
+//   warp 1      allocates TMEM, one lane issues tcgen05.mma (M=128, N=BN,
+//               K=16) for every term pair, commits each stage back to the
+//               producer and the finished accumulator to the epilogue;
+//   warps 2-5   epilogue: tcgen05.ld of the accumulator, alpha/beta, stores
+//               to column-major C (beta == 0 never reads C).
+// Every mbarrier wait is bounded; a wait that gives up records an error code
+// in the handle's device error word and the CTA drains and frees TMEM.
+//
+// The split pre-pass writes the terms as [P][rows][Kp] BF16 (K contiguous,
+// Kp = K rounded up to 64 with zeros), which also absorbs any transpose of A
+// or B, so the tensor-core kernel only ever sees K-major operands.
+#include <cuda_bf16.h>
+
+#include <mutex>
+
 #include "gemm_internal.cuh"
 #include "selector.h"
+#include "tc_ptx.cuh"
 
 namespace gb {
 
-gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t, const GemmArgs<float>&, int) {
-  return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: not built yet");
+constexpr int kTcBM = 128, kTcBK = 64, kTcThreads = 192;
+
+template <int BN, int P, int STAGES>
+struct TcCfg {
+  static constexpr int A_TILE = kTcBM * kTcBK * 2;
+  static constexpr int B_TILE = BN * kTcBK * 2;
+  static constexpr int STAGE = P * (A_TILE + B_TILE);
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static constexpr int NPAIRS = P == 1 ? 1 : (P == 2 ? 3 : 6);
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+// term pairs (a-term, b-term) with a + b <= P - 1
+__device__ __forceinline__ void term_pair(int P, int q, int& pa, int& pb) {
+  // P = 1: (0,0); P = 2: (0,0) (0,1) (1,0); P = 3: + (0,2) (1,1) (2,0)
+  const int tbl_a[6] = {0, 0, 1, 0, 1, 2};
+  const int tbl_b[6] = {0, 1, 0, 2, 1, 0};
+  (void)P;
+  pa = tbl_a[q];
+  pb = tbl_b[q];
 }
 
-int select_sgemm_method(gbblas_handle_t, const GemmArgs<float>&) { return GBBLAS_SGEMM_FP32_SIMT; }
+enum : int { kErrTcProducer = 101, kErrTcMma = 102, kErrTcEpilogue = 103, kErrTcDrain = 104 };
+
+template <int BN, int P, int STAGES>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    gemm_split_bf16_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
+                           int M, int N, int nk, float alpha, float beta, float* __restrict__ C, int64_t ldc,
+                           int* __restrict__ err) {
+  using Cfg = TcCfg<BN, P, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* tiles = smem;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * Cfg::STAGE);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accb = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kTcBM, n0 = blockIdx.x * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(accb, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, BN);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      tc::tma_prefetch_desc(&tma_a);
+      tc::tma_prefetch_desc(&tma_b);
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
+          atomicExch(err, kErrTcProducer);
+          break;
+        }
+        tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
+        uint8_t* st = tiles + s * Cfg::STAGE;
+#pragma unroll
+        for (int p = 0; p < P; ++p) tc::tma_load_3d(st + p * Cfg::A_TILE, &tma_a, &full[s], kb * kTcBK, m0, p);
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+          tc::tma_load_3d(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, &full[s], kb * kTcBK, n0, p);
+        issued = kb + 1;
+      }
+      // drain: every copy this thread issued has landed before the CTA exits
+      for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
+        if (!tc::mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1)) {
+          atomicExch(err, kErrTcDrain);
+          break;
+        }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, BN);
+      bool ok = true;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!tc::mbar_wait(&full[s], ph)) {
+          atomicExch(err, kErrTcMma);
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint8_t* st = tiles + s * Cfg::STAGE;
+#pragma unroll
+        for (int q = 0; q < Cfg::NPAIRS; ++q) {
+          int pa, pb;
+          term_pair(P, q, pa, pb);
+          const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+          const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+#pragma unroll
+          for (int j = 0; j < kTcBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
+            tc::mma_bf16(tmem, ad + 2 * j, bd + 2 * j, idesc, (kb | q | j) != 0);
+        }
+        tc::mma_commit(&empty[s]);
+      }
+      if (ok) tc::mma_commit(accb);
+    }
+  } else {
+    // epilogue warps 2..5: warp w reads TMEM lanes [32*(w%4), 32*(w%4)+32)
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int gm = m0 + row;
+    const bool ok = tc::mbar_wait(accb, 0);
+    if (!ok && lane == 0) atomicExch(err, kErrTcEpilogue);
+    tc::tc_fence_after();
+    if (ok) {
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(c0), r);
+        tc::tmem_ld_wait();
+        if (gm < M) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const int gn = n0 + c0 + i;
+            if (gn < N) {
+              float* cp = C + int64_t(gm) + int64_t(gn) * ldc;
+              float v = alpha * __uint_as_float(r[i]);
+              if (beta != 0.f) v = fmaf(beta, *cp, v);
+              *cp = v;
+            }
+          }
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, BN);
+  }
+}
+
+// ------------------------------------------------------------ split pass --
+// out[p][r][k] (k < Kp) = term p of X(r, k); X(r, k) = X[r*sr + k*sk]; zero
+// for k >= K.  32x32 tiles through shared memory so both the strided read
+// and the K-contiguous write are coalesced.
+template <int P>
+__global__ void __launch_bounds__(256) split_bf16_kernel(const float* __restrict__ X, int64_t sr, int64_t sk,
+                                                         int64_t R, int64_t K, int64_t Kp,
+                                                         __nv_bfloat16* __restrict__ out) {
+  __shared__ float t[32][33];  // t[k][r]
+  const int64_t r0 = int64_t(blockIdx.y) * 32, k0 = int64_t(blockIdx.x) * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (sr == 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t k = k0 + ty + 8 * i, r = r0 + tx;
+      t[ty + 8 * i][tx] = (r < R && k < K) ? X[r + k * sk] : 0.f;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t r = r0 + ty + 8 * i, k = k0 + tx;
+      t[tx][ty + 8 * i] = (r < R && k < K) ? X[r * sr + k * sk] : 0.f;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t r = r0 + ty + 8 * i, k = k0 + tx;
+    if (r < R && k < Kp) {
+      float x = t[tx][ty + 8 * i];
+      const int64_t o = r * Kp + k;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        out[int64_t(p) * R * Kp + o] = h;
+        x = x - __bfloat162float(h);  // exact residual
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host --
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// [P][rows][Kp] BF16 terms, box = 64 (k) x box_rows x 1
+static gbblas_status_t make_term_map(CUtensorMap* map, void* base, int64_t rows, int64_t Kp, int P, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[3] = {cuuint64_t(Kp), cuuint64_t(rows), cuuint64_t(P)};
+  cuuint64_t strides[2] = {cuuint64_t(Kp * 2), cuuint64_t(rows * Kp * 2)};
+  cuuint32_t box[3] = {cuuint32_t(kTcBK), cuuint32_t(box_rows), 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: tensor map encode failed (" + std::to_string(int(r)) + ")");
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <int P>
+static gbblas_status_t launch_split(gbblas_handle_t h, const float* X, int64_t sr, int64_t sk, int64_t R, int64_t K,
+                                    int64_t Kp, __nv_bfloat16* out) {
+  dim3 grid(unsigned(Kp / 32), unsigned(cdiv(R, 32)));
+  if (grid.y > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: too many rows");
+  split_bf16_kernel<P><<<grid, dim3(32, 8), 0, h->stream>>>(X, sr, sk, R, K, Kp, out);
+  return after_launch("split_bf16");
+}
+
+template <int BN, int P, int STAGES>
+static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb, int64_t M,
+                                 int64_t N, int64_t nk, float alpha, float beta, float* C, int64_t ldc) {
+  using Cfg = TcCfg<BN, P, STAGES>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_bf16_kernel<BN, P, STAGES>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+    attr_set = true;
+  }
+  dim3 grid(unsigned(cdiv(N, BN)), unsigned(cdiv(M, kTcBM)));
+  gemm_split_bf16_kernel<BN, P, STAGES><<<grid, kTcThreads, Cfg::SMEM, h->stream>>>(
+      ta, tb, int(M), int(N), int(nk), alpha, beta, C, ldc, h->dev_error);
+  return after_launch("gemm_split_bf16");
+}
+
+template <int P>
+static gbblas_status_t split_gemm_one(gbblas_handle_t h, const GemmArgs<float>& g, const float* A, const float* B,
+                                      float* C) {
+  const int64_t M = g.m, N = g.n, K = g.k;
+  const int64_t Kp = cdiv(K, kTcBK) * kTcBK;
+  const size_t a_bytes = size_t(P) * M * Kp * 2, b_bytes = size_t(P) * N * Kp * 2;
+  void* ws = nullptr;
+  GB_TRY(temp_acquire(h, ((a_bytes + 1023) & ~size_t(1023)) + b_bytes, &ws));
+  auto* at = static_cast<__nv_bfloat16*>(ws);
+  auto* bt = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(ws) + ((a_bytes + 1023) & ~size_t(1023)));
+  // A(m, k): (ta ? A[k + m*lda] : A[m + k*lda]);  B as rows n: (tb ? B[n + k*ldb] : B[k + n*ldb])
+  GB_TRY(launch_split<P>(h, A, g.ta ? g.lda : 1, g.ta ? 1 : g.lda, M, K, Kp, at));
+  GB_TRY(launch_split<P>(h, B, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, K, Kp, bt));
+  constexpr int BN = P == 3 ? 128 : 256;
+  constexpr int STAGES = P == 1 ? 4 : 2;
+  CUtensorMap ma, mb;
+  GB_TRY(make_term_map(&ma, at, M, Kp, P, kTcBM));
+  GB_TRY(make_term_map(&mb, bt, N, Kp, P, BN));
+  return launch_tc<BN, P, STAGES>(h, ma, mb, M, N, Kp / kTcBK, g.alpha, g.beta, C, g.ldc);
+}
+
+gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
+  if (pieces != 2 && pieces != 3) return fail(GBBLAS_STATUS_INVALID_ARG, "split-BF16 GEMM: pieces must be 2 or 3");
+  if (g.m > INT32_MAX / 2 || g.n > INT32_MAX / 2 || g.k > INT32_MAX / 2)
+    return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: dimension too large");
+  if (g.k == 0) return launch_scale_c(h, g.m, g.n, g.beta, g.c, g.ldc, g.stride_c, g.batch);
+  for (int64_t b = 0; b < g.batch; ++b) {
+    const float* A = g.a + b * g.stride_a;
+    const float* B = g.b + b * g.stride_b;
+    float* C = g.c + b * g.stride_c;
+    GB_TRY(pieces == 2 ? split_gemm_one<2>(h, g, A, B, C) : split_gemm_one<3>(h, g, A, B, C));
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+// AUTO: the FP32-accurate 3-term split on the tensor cores for single
+// problems large enough to amortise the split pass; SIMT otherwise.
+int select_sgemm_method(gbblas_handle_t, const GemmArgs<float>& g) {
+  const double work = double(g.m) * double(g.n) * double(g.k);
+  if (g.batch == 1 && g.m >= 256 && g.n >= 256 && g.k >= 128 && work >= double(1 << 27))
+    return GBBLAS_SGEMM_SPLIT_BF16X6;
+  return GBBLAS_SGEMM_FP32_SIMT;
+}
 
 }  // namespace gb

@@ -13,7 +13,23 @@ from tests.util import rng, to_dev, to_host, assert_almost_equal
 
 pytestmark = pytest.mark.gpu
 KAT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "kat.json")))
-MODES = ["fp32_simt"]
+MODES = ["fp32_simt", "split_bf16x3", "split_bf16x6"]
+U32 = 2.0 ** -24
+
+
+def norm_bound(mode, k):
+    """Componentwise bound on |C - C64| / (|alpha||A||B| + |beta C|): FP32
+    accumulation (K u) plus, for the 2-term split, the dropped 2^-16 terms."""
+    base = 2.0 * (k + 2) * U32
+    return base + (4.0 * 2.0 ** -16 if mode == "split_bf16x3" else 4.0 * U32)
+
+
+@pytest.fixture(autouse=True)
+def _reset_mode(sb):
+    yield
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    sb.check_device_error()
 
 
 def _mats(g, ta, tb, m, n, k, lda_mul, ldb_mul, ldc_mul, off, dtype):
@@ -27,7 +43,7 @@ def _mats(g, ta, tb, m, n, k, lda_mul, ldb_mul, ldc_mul, off, dtype):
 
 
 def _gemm(sb, torch, mode, ta, tb, m, n, k, alpha, beta, lda_mul=1, ldb_mul=1, ldc_mul=1, off=0,
-          dtype=np.float32, seed=0, c_nan=False):
+          dtype=np.float32, seed=0, c_nan=False, want_scale=False):
     from portblas_gb300 import blas
     g = rng(seed + m * 3 + n * 5 + k * 7)
     a, lda, b, ldb, c, ldc = _mats(g, ta, tb, m, n, k, lda_mul, ldb_mul, ldc_mul, off, dtype)
@@ -47,6 +63,9 @@ def _gemm(sb, torch, mode, ta, tb, m, n, k, alpha, beta, lda_mul=1, ldb_mul=1, l
     win[:m] = got
     np.testing.assert_array_equal(np.isnan(out), np.isnan(full))
     np.testing.assert_array_equal(np.nan_to_num(out), np.nan_to_num(full))
+    if want_scale:
+        scale = oracle.gemm_absscale(ta, tb, m, n, k, alpha, a[off:], lda, b[off:], ldb, beta, c[off:], ldc)
+        return got, ref, scale
     return got, ref
 
 
@@ -56,9 +75,10 @@ def _gemm(sb, torch, mode, ta, tb, m, n, k, alpha, beta, lda_mul=1, ldb_mul=1, l
                                    (129, 257, 64)])
 @pytest.mark.parametrize("alpha,beta", [(1.5, 0.0), (1.0, 1.0), (1.5, 1.5), (0.0, 1.5)])
 def test_gemm_sweep(sb, torch_cuda, mode, ta, tb, m, n, k, alpha, beta):
-    got, ref = _gemm(sb, torch_cuda, mode, ta, tb, m, n, k, alpha, beta)
+    got, ref, scale = _gemm(sb, torch_cuda, mode, ta, tb, m, n, k, alpha, beta, want_scale=True)
     assert_almost_equal(got, ref)
-    np.testing.assert_allclose(got, ref, rtol=1e-5 * np.sqrt(k), atol=1e-5 * np.sqrt(k) * 25 * k)
+    err = np.abs(got - ref) / np.maximum(scale, 1e-300)
+    assert err.max() <= norm_bound(mode, k), (mode, float(err.max()))
 
 
 @pytest.mark.parametrize("mode", MODES)
