@@ -157,7 +157,7 @@ def run_step(blas, sb, inp, outs, events=None):
     return [n for n, _ in ops]
 
 
-def bench_memory_set(torch, blas, sb, steps, warmup, dev):
+def bench_memory_set(torch, blas, sb, steps, warmup, dev, per_op_reps=None):
     inp = make_inputs(torch, dev)
     outs = dict(yn=torch.empty(GEMV_N, device=dev), yt=torch.empty(GEMV_N, device=dev),
                 s=torch.zeros(3, device=dev), i=torch.zeros(2, dtype=torch.int32, device=dev),
@@ -168,7 +168,8 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev):
     torch.cuda.synchronize()
     # per-op device times (events around each op, separate pass)
     per_op = {n: [] for n in names}
-    for _ in range(max(3, min(steps, 10))):
+    reps = max(3, min(steps, 10)) if per_op_reps is None else per_op_reps
+    for _ in range(reps):
         ev = {n: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for n in names}
         run_step(blas, sb, inp, outs, ev)
         torch.cuda.synchronize()
@@ -191,7 +192,8 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev):
     # correctness spot checks of the last step
     iam = outs["i"].cpu().numpy()
     checks = {"iamax_index": int(iam[0]), "iamax_expected_first_planted": inp["planted"]}
-    return dict(ms=ms, per_op={n: statistics.median(v) for n, v in per_op.items()}, launches=launches,
+    return dict(ms=ms, per_op={n: statistics.median(v) if v else None for n, v in per_op.items()},
+                launches=launches,
                 clocks=clk.summary(), checks=checks, inp=inp, outs=outs)
 
 
@@ -233,11 +235,11 @@ def bench_e2e(torch, blas, sb, steps, warmup, dev):
     return dict(ms=start.elapsed_time(end) / steps, h2d=h2d, d2h=d2h)
 
 
-def bench_sgemm(torch, blas, sb, dev, reps=3):
-    """8192^3 FP32 GEMM: plain SIMT vs split-BF16 (x3 and x6 products), NN and TN,
-    entries s*2^u (u ~ U[-10, 10]); error vs the FP64 oracle on sampled entries."""
+def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
+    """n^3 FP32 GEMM (n = 8192 by default): plain SIMT vs split-BF16 (x3 and x6
+    products), NN and TN, entries s*2^u (u ~ U[-10, 10]); error vs the FP64
+    oracle on sampled entries."""
     import oracle
-    n = 8192
     g = np.random.default_rng(99)
 
     def pw2(size):
@@ -284,6 +286,8 @@ def bench_sgemm(torch, blas, sb, dev, reps=3):
                 "max_norm_err": float(np.max(err / scale)), "mean_norm_err": float(np.mean(err / scale)),
                 "sampled_entries": len(rows)}
     sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    if not with_dgemm:
+        return res
     # DGEMM 4096^3 on the FP64 pipe
     nd = 4096
     A = torch.rand(nd * nd, device=dev, dtype=torch.float64) * 2 - 1
@@ -364,6 +368,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-sgemm", action="store_true", help="skip the SGEMM/DGEMM set")
+    ap.add_argument("--profile", choices=["memory", "sgemm"], default=None,
+                    help="short run of one workload only (no e2e, CPU baseline or JSON line), for ncu captures")
+    ap.add_argument("--sgemm-n", type=int, default=8192)
     args = ap.parse_args()
     warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
@@ -402,6 +409,14 @@ def main():
     __graft_entry__.build()
     from portblas_gb300 import blas
     sb = blas.SB_Handle()
+    if args.profile == "memory":
+        r = bench_memory_set(torch, blas, sb, args.steps, args.warmup, dev, per_op_reps=0)
+        print(json.dumps({"profile": "memory", "ms_per_step": r["ms"]}))
+        return
+    if args.profile == "sgemm":
+        r = bench_sgemm(torch, blas, sb, dev, reps=1, n=args.sgemm_n, with_dgemm=False)
+        print(json.dumps({"profile": "sgemm", "n": args.sgemm_n, "res": r}))
+        return
     mem = bench_memory_set(torch, blas, sb, args.steps, warmup, dev)
     e2e = bench_e2e(torch, blas, sb, max(3, args.steps // 4), 3, dev)
     ms = mem["ms"]

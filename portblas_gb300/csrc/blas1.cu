@@ -30,6 +30,15 @@ struct AsumOp {
   __device__ static Acc init() { return Acc::zero(); }
   using Out = T;
   __device__ static void add(Acc& a, T x, T, int64_t) { a.add(fabs(x)); }
+  // one 128-bit packet: plain sum of the (at most 4) magnitudes, then one
+  // compensated addition
+  template <int W>
+  __device__ static void add_vec(Acc& a, const T* x, const T*, int64_t) {
+    T s = fabs(x[0]);
+#pragma unroll
+    for (int e = 1; e < W; ++e) s += fabs(x[e]);
+    a.add(s);
+  }
   __device__ static void combine(Acc& a, const Acc& b) { a.merge(b); }
   __device__ static Acc shfl(const Acc& a, int off) { return a.shfl_down(off); }
   __device__ static void finish(const Acc& a, Out* r) { *r = a.value(); }
@@ -43,6 +52,11 @@ struct DotOp {
   __device__ static Acc init() { return Acc::zero(); }
   using Out = T;
   __device__ static void add(Acc& a, T x, T y, int64_t) { a.add_product(x, y); }
+  template <int W>
+  __device__ static void add_vec(Acc& a, const T* x, const T* y, int64_t) {
+#pragma unroll
+    for (int e = 0; e < W; ++e) a.add_product(x[e], y[e]);
+  }
   __device__ static void combine(Acc& a, const Acc& b) { a.merge(b); }
   __device__ static Acc shfl(const Acc& a, int off) { return a.shfl_down(off); }
   __device__ static void finish(const Acc& a, Out* r) { *r = a.value(); }
@@ -106,6 +120,26 @@ struct Nrm2Op {
       a.sml = fma(s, s, a.sml);
     } else {
       a.med.add(ax * ax);  // NaN lands here and propagates, as it must
+    }
+  }
+  // one packet: when every |x| is in the medium range (the common case) the
+  // squares are summed plainly and added once with compensation
+  template <int W>
+  __device__ static void add_vec(Acc& a, const T* x, const T* y, int64_t i) {
+    T lo = fabs(x[0]), hi = lo;
+#pragma unroll
+    for (int e = 1; e < W; ++e) {
+      lo = fmin(lo, fabs(x[e]));
+      hi = fmax(hi, fabs(x[e]));
+    }
+    if (lo >= C::tsml && hi <= C::tbig) {
+      T s = x[0] * x[0];
+#pragma unroll
+      for (int e = 1; e < W; ++e) s = fma(x[e], x[e], s);
+      a.med.add(s);
+    } else {
+#pragma unroll
+      for (int e = 0; e < W; ++e) add(a, x[e], y ? y[e] : T(0), i + e);
     }
   }
   __device__ static void combine(Acc& a, const Acc& b) {
@@ -185,9 +219,14 @@ struct IdxAcc {
 template <typename T, bool IS_MAX>
 struct IamaxOp {
   using Acc = IdxAcc<T>;
+  // The walk of one thread visits increasing indices, so within a thread a
+  // strict comparison keeps the first index of a tie.  The thread-level
+  // initial value sits just outside portBLAS's initial tuple: -1 below
+  // IMax's 0 (so |x| == 0 still wins) and +inf above IMin's T max (so
+  // |x| == T max still wins while inf, like in portBLAS, never does).
   __device__ static Acc init() {
     Acc a;
-    a.v = IS_MAX ? T(0) : (sizeof(T) == 4 ? T(FLT_MAX) : T(DBL_MAX));
+    a.v = IS_MAX ? T(-1) : T(INFINITY);
     a.i = kNoIndex;
     return a;
   }
@@ -198,10 +237,15 @@ struct IamaxOp {
   }
   __device__ static void add(Acc& a, T x, T, int64_t idx) {
     T ax = fabs(x);
-    if (better(ax, idx, a.v, a.i)) {
+    if (IS_MAX ? (ax > a.v) : (ax < a.v)) {
       a.v = ax;
       a.i = idx;
     }
+  }
+  template <int W>
+  __device__ static void add_vec(Acc& a, const T* x, const T*, int64_t i) {
+#pragma unroll
+    for (int e = 0; e < W; ++e) add(a, x[e], T(0), i + e);
   }
   __device__ static void combine(Acc& a, const Acc& b) {
     if (better(b.v, b.i, a.v, a.i)) a = b;
@@ -256,7 +300,7 @@ __device__ __forceinline__ typename Op::Acc block_reduce(typename Op::Acc a, typ
 // VEC: x (and y) contiguous and 16-byte aligned; otherwise strided scalar
 // loads from the view base (negative increments allowed).
 template <class Op, typename T, bool VEC, bool HAS_Y>
-__global__ void __launch_bounds__(kThreads) blas1_reduce(int64_t n, const T* __restrict__ x, int64_t incx,
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) blas1_reduce(int64_t n, const T* __restrict__ x, int64_t incx,
                                                          const T* __restrict__ y, int64_t incy,
                                                          typename Op::Acc* __restrict__ partials,
                                                          unsigned int* __restrict__ ticket,
@@ -288,16 +332,14 @@ __global__ void __launch_bounds__(kThreads) blas1_reduce(int64_t n, const T* __r
         T xe[W], ye[W];
         V::unpack(xr[u], xe);
         if (HAS_Y) V::unpack(yr[u], ye);
-#pragma unroll
-        for (int e = 0; e < W; ++e) Op::add(acc, xe[e], HAS_Y ? ye[e] : T(0), (v + u * nthreads) * W + e);
+        Op::template add_vec<W>(acc, xe, HAS_Y ? ye : nullptr, (v + u * nthreads) * W);
       }
     }
     for (; v < nv; v += nthreads) {
       T xe[W], ye[W];
       V::unpack(__ldcs(xv + v), xe);
       if (HAS_Y) V::unpack(__ldcs(yv + v), ye);
-#pragma unroll
-      for (int e = 0; e < W; ++e) Op::add(acc, xe[e], HAS_Y ? ye[e] : T(0), v * W + e);
+      Op::template add_vec<W>(acc, xe, HAS_Y ? ye : nullptr, v * W);
     }
     // scalar tail, taken by the threads that follow in grid order
     for (int64_t i = nv * W + tid; i < n; i += nthreads) Op::add(acc, x[i], HAS_Y ? y[i] : T(0), i);
