@@ -122,10 +122,11 @@ def make_inputs(torch, dev):
     xg = torch.rand(GEMV_N, device=dev, generator=gen) * 2 - 1
     v = torch.randn(VEC_N, device=dev, generator=gen)
     w = torch.randn(VEC_N, device=dev, generator=gen)
-    # plant the largest |x| at 8 random indices with random signs
-    idx = torch.randperm(VEC_N, device=dev, generator=gen)[:8]
+    # plant the largest |x| at 8 distinct random indices with random signs
+    pick = np.random.default_rng(20240917)
+    idx = torch.from_numpy(pick.choice(VEC_N, size=8, replace=False).astype(np.int64)).to(dev)
     big = 8.0 * v.abs().max()
-    signs = torch.where(torch.rand(8, device=dev, generator=gen) < 0.5, -1.0, 1.0)
+    signs = torch.from_numpy(pick.choice([-1.0, 1.0], size=8).astype(np.float32)).to(dev)
     v[idx] = big * signs
     R = torch.rand(RED_N * RED_N, device=dev, generator=gen) * 2 - 1
     return dict(A=A, xg=xg, v=v, w=w, R=R, planted=int(idx.min().item()))

@@ -212,6 +212,20 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
                                     const void* const* b, const int64_t* ldb, const float* beta, float* const* c,
                                     const int64_t* ldc);
 
+/* A reusable grouped GEMM: the problem table is uploaded once and every run
+ * replays one CUDA graph holding the persistent launch (no host work per
+ * run beyond cudaGraphLaunch).  Pointers and sizes are fixed at creation;
+ * the data behind them may change between runs. */
+typedef struct gbblas_grouped_plan_s* gbblas_grouped_plan_t;
+gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t count, const char* transa,
+                                           const char* transb, const int64_t* m, const int64_t* n,
+                                           const int64_t* k, const float* alpha, const void* const* a,
+                                           const int64_t* lda, const void* const* b, const int64_t* ldb,
+                                           const float* beta, float* const* c, const int64_t* ldc,
+                                           gbblas_grouped_plan_t* plan);
+gbblas_status_t gbblas_grouped_plan_run(gbblas_handle_t h, gbblas_grouped_plan_t plan);
+gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t plan);
+
 /* ------------------------------------------------------------ extension -- */
 /* blas::extension::_reduction<op, T> (include/interface/extension_interface.h:453-462;
  *   src/interface/extension_interface.hpp:344-409, 578-593;

@@ -1,0 +1,316 @@
+/*
+ * portblas_gb.h — header-only C++ shim that re-creates portBLAS's `blas::`
+ * interface for the hot path on top of the gbblas C ABI (gbblas.h).
+ *
+ * Source written against portBLAS compiles unchanged for these calls: the
+ * function names, template shapes, argument order and meaning follow
+ *   include/interface/blas1_interface.h   (_asum, _nrm2, _dot, _iamax, _iamin)
+ *   include/interface/blas2_interface.h   (_gemv)
+ *   include/interface/blas3_interface.h   (_gemm, _gemm_batched, _gemm_strided_batched)
+ *   include/interface/extension_interface.h (extension::_reduction)
+ * and the errors are the same exception types (std::invalid_argument,
+ * blas::unsupported_exception).  Differences a caller can observe:
+ *   - SB_Handle wraps a cudaStream_t instead of a sycl::queue, and buffers are
+ *     device pointers (portBLAS's USM mode); there is no BufferIterator.
+ *   - event_t is a vector of cudaEvent_t.  Each call makes its stream wait on
+ *     the dependency events and returns one event recorded after its work;
+ *     returned events come from a ring of kEventRing per handle and stay valid
+ *     for the next kEventRing - 1 calls on that handle.
+ *   - the async BLAS-1 reductions overwrite the result (portBLAS adds into it).
+ */
+#ifndef PORTBLAS_GB_H
+#define PORTBLAS_GB_H
+
+#include <cuda_runtime_api.h>
+
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "gbblas.h"
+
+namespace blas {
+
+enum class transpose_type : char { Normal = 'n', Transposed = 't', Conjugate = 'c' };
+enum class gemm_batch_type_t : int { strided = 0, interleaved = 1 };
+enum class reduction_dim_t : int { inner = 0, outer = 1 };
+
+/* include/blas_meta.h:225-235 */
+class unsupported_exception : public std::runtime_error {
+ public:
+  explicit unsupported_exception(const std::string& what) : std::runtime_error(what) {}
+};
+
+/* operator tags of extension::_reduction (src/operations/blas_operators.hpp:149-274) */
+struct AddOperator { static constexpr int code = GBBLAS_OP_ADD; };
+struct ProductOperator { static constexpr int code = GBBLAS_OP_PRODUCT; };
+struct MaxOperator { static constexpr int code = GBBLAS_OP_MAX; };
+struct MinOperator { static constexpr int code = GBBLAS_OP_MIN; };
+struct AbsoluteAddOperator { static constexpr int code = GBBLAS_OP_ABS_ADD; };
+struct MeanOperator { static constexpr int code = GBBLAS_OP_MEAN; };
+
+namespace detail {
+inline void check(gbblas_status_t s) {
+  if (s == GBBLAS_STATUS_SUCCESS) return;
+  std::string msg = gbblas_last_error();
+  if (msg.empty()) msg = gbblas_status_string(s);
+  switch (s) {
+    case GBBLAS_STATUS_INVALID_ARG: throw std::invalid_argument(msg);
+    case GBBLAS_STATUS_UNSUPPORTED: throw unsupported_exception(msg);
+    default: throw std::runtime_error(msg);
+  }
+}
+template <typename C>
+using elem_t = std::remove_cv_t<std::remove_pointer_t<C>>;
+}  // namespace detail
+
+/* blas::SB_Handle (include/sb_handle/portblas_handle.h:46-200) over a CUDA stream. */
+class SB_Handle {
+ public:
+  using event_t = std::vector<cudaEvent_t>;
+  static constexpr int kEventRing = 64;
+
+  explicit SB_Handle(cudaStream_t stream = nullptr) : stream_(stream) {
+    detail::check(gbblas_handle_create(static_cast<void*>(stream), &h_));
+    for (auto& e : ring_)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        throw std::runtime_error("SB_Handle: cudaEventCreate failed");
+  }
+  ~SB_Handle() {
+    for (auto& e : ring_)
+      if (e) cudaEventDestroy(e);
+    gbblas_handle_destroy(h_);
+  }
+  SB_Handle(const SB_Handle&) = delete;
+  SB_Handle& operator=(const SB_Handle&) = delete;
+
+  cudaStream_t get_queue() const { return stream_; }
+  gbblas_handle_t native() const { return h_; }
+  void wait() { detail::check(gbblas_wait(h_)); }
+  void wait(const event_t& evs) {
+    for (auto e : evs)
+      if (cudaEventSynchronize(e) != cudaSuccess) throw std::runtime_error("SB_Handle::wait: event failed");
+  }
+  void set_sgemm_mode(gbblas_sgemm_mode_t m) { detail::check(gbblas_set_sgemm_mode(h_, m)); }
+
+  // stream waits for the dependencies; returns an event after `status`'s work
+  void depend(const event_t& deps) {
+    for (auto e : deps)
+      if (e && cudaStreamWaitEvent(stream_, e, 0) != cudaSuccess)
+        throw std::runtime_error("SB_Handle: cudaStreamWaitEvent failed");
+  }
+  event_t done(gbblas_status_t status) {
+    detail::check(status);
+    cudaEvent_t e = ring_[next_++ % kEventRing];
+    if (cudaEventRecord(e, stream_) != cudaSuccess) throw std::runtime_error("SB_Handle: cudaEventRecord failed");
+    return event_t{e};
+  }
+
+ private:
+  cudaStream_t stream_;
+  gbblas_handle_t h_ = nullptr;
+  cudaEvent_t ring_[kEventRing] = {};
+  unsigned next_ = 0;
+};
+
+/* ------------------------------------------------------------------ BLAS-3 */
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename container_2_t,
+          typename element_t, typename index_t>
+typename sb_handle_t::event_t _gemm(sb_handle_t& sb, char ta, char tb, index_t M, index_t N, index_t K,
+                                    element_t alpha, container_0_t a, index_t lda, container_1_t b, index_t ldb,
+                                    element_t beta, container_2_t c, index_t ldc,
+                                    const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_2_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_sgemm(sb.native(), ta, tb, M, N, K, float(alpha), a, lda, b, ldb, float(beta), c, ldc));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dgemm(sb.native(), ta, tb, M, N, K, double(alpha), a, lda, b, ldb, double(beta), c, ldc));
+  else
+    throw unsupported_exception("_gemm: element type not supported");
+}
+
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename container_2_t,
+          typename element_t, typename index_t>
+typename sb_handle_t::event_t _gemm_batched(sb_handle_t& sb, char ta, char tb, index_t M, index_t N, index_t K,
+                                            element_t alpha, container_0_t a, index_t lda, container_1_t b,
+                                            index_t ldb, element_t beta, container_2_t c, index_t ldc,
+                                            index_t batch_size,
+                                            gemm_batch_type_t batch_type = gemm_batch_type_t::strided,
+                                            const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_2_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_sgemm_batched(sb.native(), ta, tb, M, N, K, float(alpha), a, lda, b, ldb, float(beta), c,
+                                        ldc, batch_size, int(batch_type)));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dgemm_batched(sb.native(), ta, tb, M, N, K, double(alpha), a, lda, b, ldb, double(beta),
+                                        c, ldc, batch_size, int(batch_type)));
+  else
+    throw unsupported_exception("_gemm_batched: element type not supported");
+}
+
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename container_2_t,
+          typename element_t, typename index_t>
+typename sb_handle_t::event_t _gemm_strided_batched(sb_handle_t& sb, char ta, char tb, index_t M, index_t N,
+                                                    index_t K, element_t alpha, container_0_t a, index_t lda,
+                                                    index_t stridea, container_1_t b, index_t ldb, index_t strideb,
+                                                    element_t beta, container_2_t c, index_t ldc, index_t stridec,
+                                                    index_t batch_size,
+                                                    const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_2_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_sgemm_strided_batched(sb.native(), ta, tb, M, N, K, float(alpha), a, lda, stridea, b, ldb,
+                                                strideb, float(beta), c, ldc, stridec, batch_size));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dgemm_strided_batched(sb.native(), ta, tb, M, N, K, double(alpha), a, lda, stridea, b,
+                                                ldb, strideb, double(beta), c, ldc, stridec, batch_size));
+  else
+    throw unsupported_exception("_gemm_strided_batched: element type not supported");
+}
+
+/* ------------------------------------------------------------------ BLAS-2 */
+template <typename sb_handle_t, typename index_t, typename element_t, typename container_t0,
+          typename container_t1, typename increment_t, typename container_t2>
+typename sb_handle_t::event_t _gemv(sb_handle_t& sb, char trans, index_t M, index_t N, element_t alpha,
+                                    container_t0 a, index_t lda, container_t1 x, increment_t incx, element_t beta,
+                                    container_t2 y, increment_t incy,
+                                    const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_t2>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_sgemv(sb.native(), trans, M, N, float(alpha), a, lda, x, incx, float(beta), y, incy));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dgemv(sb.native(), trans, M, N, double(alpha), a, lda, x, incx, double(beta), y, incy));
+  else
+    throw unsupported_exception("_gemv: element type not supported");
+}
+
+/* ------------------------------------------------------------------ BLAS-1 */
+#define PORTBLAS_GB_RED1(NAME)                                                                               \
+  template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename index_t,           \
+            typename increment_t>                                                                            \
+  typename sb_handle_t::event_t _##NAME(sb_handle_t& sb, index_t N, container_0_t x, increment_t incx,        \
+                                        container_1_t rs, const typename sb_handle_t::event_t& deps = {}) {   \
+    using T = detail::elem_t<container_0_t>;                                                                 \
+    sb.depend(deps);                                                                                          \
+    if constexpr (std::is_same_v<T, float>)                                                                  \
+      return sb.done(gbblas_s##NAME(sb.native(), N, x, incx, rs));                                           \
+    else if constexpr (std::is_same_v<T, double>)                                                            \
+      return sb.done(gbblas_d##NAME(sb.native(), N, x, incx, rs));                                           \
+    else                                                                                                      \
+      throw unsupported_exception(#NAME ": element type not supported");                                     \
+  }                                                                                                           \
+  template <typename sb_handle_t, typename container_t, typename index_t, typename increment_t>              \
+  detail::elem_t<container_t> _##NAME(sb_handle_t& sb, index_t N, container_t x, increment_t incx,           \
+                                      const typename sb_handle_t::event_t& deps = {}) {                      \
+    using T = detail::elem_t<container_t>;                                                                   \
+    sb.depend(deps);                                                                                          \
+    T r{};                                                                                                    \
+    if constexpr (std::is_same_v<T, float>)                                                                  \
+      detail::check(gbblas_s##NAME##_sync(sb.native(), N, x, incx, &r));                                     \
+    else if constexpr (std::is_same_v<T, double>)                                                            \
+      detail::check(gbblas_d##NAME##_sync(sb.native(), N, x, incx, &r));                                     \
+    else                                                                                                      \
+      throw unsupported_exception(#NAME ": element type not supported");                                     \
+    return r;                                                                                                 \
+  }
+
+/* _asum: include/interface/blas1_interface.h:631-637 (async), :979-984 (sync) */
+PORTBLAS_GB_RED1(asum)
+/* _nrm2: include/interface/blas1_interface.h:712-718 (async), :995-1000 (sync) */
+PORTBLAS_GB_RED1(nrm2)
+#undef PORTBLAS_GB_RED1
+
+/* _dot: include/interface/blas1_interface.h:582-588 (async), :903-909 (sync) */
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename container_2_t,
+          typename index_t, typename increment_t>
+typename sb_handle_t::event_t _dot(sb_handle_t& sb, index_t N, container_0_t x, increment_t incx,
+                                   container_1_t y, increment_t incy, container_2_t rs,
+                                   const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_0_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_sdot(sb.native(), N, x, incx, y, incy, rs));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_ddot(sb.native(), N, x, incx, y, incy, rs));
+  else
+    throw unsupported_exception("_dot: element type not supported");
+}
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename index_t,
+          typename increment_t>
+detail::elem_t<container_0_t> _dot(sb_handle_t& sb, index_t N, container_0_t x, increment_t incx, container_1_t y,
+                                   increment_t incy, const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_0_t>;
+  sb.depend(deps);
+  T r{};
+  if constexpr (std::is_same_v<T, float>)
+    detail::check(gbblas_sdot_sync(sb.native(), N, x, incx, y, incy, &r));
+  else if constexpr (std::is_same_v<T, double>)
+    detail::check(gbblas_ddot_sync(sb.native(), N, x, incx, y, incy, &r));
+  else
+    throw unsupported_exception("_dot: element type not supported");
+  return r;
+}
+
+/* _iamax / _iamin: include/interface/blas1_interface.h:646-666 (async, int
+ * result), :949-968 (sync) */
+#define PORTBLAS_GB_IAM(NAME, S, D)                                                                          \
+  template <typename sb_handle_t, typename container_t, typename ContainerI, typename index_t,                 \
+            typename increment_t>                                                                            \
+  typename sb_handle_t::event_t NAME(sb_handle_t& sb, index_t N, container_t x, increment_t incx,            \
+                                     ContainerI rs, const typename sb_handle_t::event_t& deps = {}) {        \
+    using T = detail::elem_t<container_t>;                                                                   \
+    static_assert(sizeof(detail::elem_t<ContainerI>) == 4, #NAME ": the index result is 32-bit");            \
+    sb.depend(deps);                                                                                          \
+    int32_t* r = reinterpret_cast<int32_t*>(rs);                                                             \
+    if constexpr (std::is_same_v<T, float>)                                                                  \
+      return sb.done(S(sb.native(), N, x, incx, r));                                                         \
+    else if constexpr (std::is_same_v<T, double>)                                                            \
+      return sb.done(D(sb.native(), N, x, incx, r));                                                         \
+    else                                                                                                      \
+      throw unsupported_exception(#NAME ": element type not supported");                                     \
+  }                                                                                                           \
+  template <typename sb_handle_t, typename container_t, typename index_t, typename increment_t>              \
+  index_t NAME(sb_handle_t& sb, index_t N, container_t x, increment_t incx,                                  \
+               const typename sb_handle_t::event_t& deps = {}) {                                             \
+    using T = detail::elem_t<container_t>;                                                                   \
+    sb.depend(deps);                                                                                          \
+    int32_t r = 0;                                                                                            \
+    if constexpr (std::is_same_v<T, float>)                                                                  \
+      detail::check(S##_sync(sb.native(), N, x, incx, &r));                                                  \
+    else if constexpr (std::is_same_v<T, double>)                                                            \
+      detail::check(D##_sync(sb.native(), N, x, incx, &r));                                                  \
+    else                                                                                                      \
+      throw unsupported_exception(#NAME ": element type not supported");                                     \
+    return static_cast<index_t>(r);                                                                          \
+  }
+PORTBLAS_GB_IAM(_iamax, gbblas_isamax, gbblas_idamax)
+PORTBLAS_GB_IAM(_iamin, gbblas_isamin, gbblas_idamin)
+#undef PORTBLAS_GB_IAM
+
+/* --------------------------------------------------------------- extension */
+namespace extension {
+/* include/interface/extension_interface.h:453-462 */
+template <typename operator_t, typename element_t, typename sb_handle_t, typename input_t, typename output_t,
+          typename index_t>
+typename sb_handle_t::event_t _reduction(sb_handle_t& sb, input_t buffer_in, index_t ld, output_t buffer_out,
+                                         index_t rows, index_t cols, reduction_dim_t reduction_dim,
+                                         const typename sb_handle_t::event_t& deps = {}) {
+  sb.depend(deps);
+  if constexpr (std::is_same_v<element_t, float>)
+    return sb.done(gbblas_sreduction(sb.native(), operator_t::code, int(reduction_dim), buffer_in, ld, buffer_out,
+                                     rows, cols));
+  else if constexpr (std::is_same_v<element_t, double>)
+    return sb.done(gbblas_dreduction(sb.native(), operator_t::code, int(reduction_dim), buffer_in, ld, buffer_out,
+                                     rows, cols));
+  else
+    throw unsupported_exception("_reduction: element type not supported");
+}
+}  // namespace extension
+
+}  // namespace blas
+
+#endif  // PORTBLAS_GB_H

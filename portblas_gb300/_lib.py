@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libgbblas.so")
 
 _TYPES = {
     "gbblas_handle_t": C.c_void_p,
+    "gbblas_grouped_plan_t": C.c_void_p,
     "int64_t": C.c_int64,
     "int32_t": C.c_int32,
     "int": C.c_int,

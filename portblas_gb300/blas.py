@@ -297,14 +297,11 @@ class extension:
 
 
 # --------------------------------------------------------- grouped GEMM --
-def _gemm_grouped(sb_handle, problems, dtype="float32"):
-    """Grouped GEMM over uneven problems (no portBLAS counterpart).
+_DTYPE_CODES = {"float32": 0, "bfloat16": 1, "torch.float32": 0, "torch.bfloat16": 1}
 
-    ``problems`` is a list of dicts with keys transa, transb, m, n, k, alpha,
-    a, lda, b, ldb, beta, c, ldc (a/b/c CUDA tensors or addresses)."""
+
+def _grouped_arrays(problems):
     cnt = len(problems)
-    codes = {"float32": 0, "bfloat16": 1, "torch.float32": 0, "torch.bfloat16": 1}
-    dt = codes[str(dtype)]
     I64 = C.c_int64 * cnt
     F32 = C.c_float * cnt
     VP = C.c_void_p * cnt
@@ -317,6 +314,44 @@ def _gemm_grouped(sb_handle, problems, dtype="float32"):
         c=VP(*[_ptr(p["c"]) for p in problems]), lda=I64(*[p["lda"] for p in problems]),
         ldb=I64(*[p["ldb"] for p in problems]), ldc=I64(*[p["ldc"] for p in problems]))
     A = lambda x: C.addressof(x)
-    return _call("gbblas_gemm_grouped", sb_handle.handle, dt, cnt, A(ta), A(tb), A(arrs["m"]), A(arrs["n"]),
-                 A(arrs["k"]), A(arrs["alpha"]), A(arrs["a"]), A(arrs["lda"]), A(arrs["b"]), A(arrs["ldb"]),
-                 A(arrs["beta"]), A(arrs["c"]), A(arrs["ldc"]))
+    keep = (ta, tb, arrs)
+    args = (cnt, A(ta), A(tb), A(arrs["m"]), A(arrs["n"]), A(arrs["k"]), A(arrs["alpha"]), A(arrs["a"]),
+            A(arrs["lda"]), A(arrs["b"]), A(arrs["ldb"]), A(arrs["beta"]), A(arrs["c"]), A(arrs["ldc"]))
+    return args, keep
+
+
+def _gemm_grouped(sb_handle, problems, dtype="float32"):
+    """Grouped GEMM over uneven problems (no portBLAS counterpart), one
+    persistent launch.  ``problems`` is a list of dicts with keys transa,
+    transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc (a/b/c CUDA tensors or
+    addresses); A and B are ``dtype`` (float32 or bfloat16), C is float32."""
+    args, keep = _grouped_arrays(problems)
+    return _call("gbblas_gemm_grouped", sb_handle.handle, _DTYPE_CODES[str(dtype)], *args)
+
+
+class GroupedPlan:
+    """A reusable grouped GEMM replayed from a CUDA graph
+    (gbblas_grouped_plan_create / _run / _destroy)."""
+
+    def __init__(self, sb_handle, problems, dtype="float32"):
+        self._L = _lib.load()
+        self.sb = sb_handle
+        args, self._keep = _grouped_arrays(problems)
+        p = C.c_void_p()
+        _check(self._L.gbblas_grouped_plan_create(sb_handle.handle, _DTYPE_CODES[str(dtype)], *args, C.byref(p)))
+        self._p = p
+
+    def run(self):
+        _check(self._L.gbblas_grouped_plan_run(self.sb.handle, self._p))
+        return []
+
+    def close(self):
+        if getattr(self, "_p", None) is not None and self._p.value:
+            self._L.gbblas_grouped_plan_destroy(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

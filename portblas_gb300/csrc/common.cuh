@@ -79,7 +79,7 @@ gbblas_status_t temp_acquire(gbblas_handle_t h, size_t bytes, void** ptr);
 // Number of ticket counters available: kMaxTickets.
 constexpr size_t kMaxTickets = 1u << 16;
 
-inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // Element i of a strided vector view (portBLAS VectorView, src/views/view.hpp:43-48).
 template <typename T>

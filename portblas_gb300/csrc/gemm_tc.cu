@@ -4,16 +4,19 @@
 // x_{i+1} = bf16(x - x0 - ... - x_i) (exact residuals in FP32).  The product
 // keeps the terms whose order is at least 2^-16 (P = 2: x0y0, x0y1, x1y0) or
 // 2^-24 (P = 3: the six terms with i + j <= 2); every BF16 x BF16 product is
-// exact and all of them accumulate in one FP32 accumulator in tensor memory.
+// exact and they accumulate in FP32, first in tensor memory per k-chunk, then
+// in registers across chunks.
 //
 // Pipeline per CTA (128 x BN output tile, BK = 64):
 //   warp 0      TMA producer: the P A-term tiles and P B-term tiles of one
 //               k-block per stage (128-byte swizzle, K-major);
 //   warp 1      allocates TMEM, one lane issues tcgen05.mma (M=128, N=BN,
 //               K=16) for every term pair, commits each stage back to the
-//               producer and the finished accumulator to the epilogue;
-//   warps 2-5   epilogue: tcgen05.ld of the accumulator, alpha/beta, stores
-//               to column-major C (beta == 0 never reads C).
+//               producer and each finished k-chunk accumulator (two TMEM
+//               buffers) to the epilogue;
+//   warps 2-5   epilogue: tcgen05.ld of each chunk into a per-thread FP32
+//               row, then alpha/beta and stores to column-major C (beta == 0
+//               never reads C).
 // Every mbarrier wait is bounded; a wait that gives up records an error code
 // in the handle's device error word and the CTA drains and frees TMEM.
 //
@@ -39,21 +42,29 @@ struct TcCfg {
   static constexpr int STAGE = P * (A_TILE + B_TILE);
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
   static constexpr int NPAIRS = P == 1 ? 1 : (P == 2 ? 3 : 6);
+  static constexpr int TMEM_COLS = 2 * BN;  // two chunk accumulators
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
+  static_assert(TMEM_COLS <= 512, "tensor memory budget");
 };
 
-// term pairs (a-term, b-term) with a + b <= P - 1
-__device__ __forceinline__ void term_pair(int P, int q, int& pa, int& pb) {
-  // P = 1: (0,0); P = 2: (0,0) (0,1) (1,0); P = 3: + (0,2) (1,1) (2,0)
-  const int tbl_a[6] = {0, 0, 1, 0, 1, 2};
-  const int tbl_b[6] = {0, 1, 0, 2, 1, 0};
-  (void)P;
-  pa = tbl_a[q];
-  pb = tbl_b[q];
+// k-blocks (of 64) accumulated in tensor memory before the partial sum is
+// promoted into the FP32 register accumulator of the epilogue warps
+constexpr int kTcChunk = 4;
+
+// term pairs (a-term, b-term) with a + b <= P - 1, largest first:
+// P = 1: (0,0); P = 2: (0,0) (0,1) (1,0); P = 3: + (0,2) (1,1) (2,0)
+__device__ __forceinline__ void term_pair(int q, int& pa, int& pb) {
+  pa = (q == 2 || q == 4) ? 1 : (q == 5 ? 2 : 0);
+  pb = (q == 1 || q == 4) ? 1 : (q == 3 ? 2 : 0);
 }
 
 enum : int { kErrTcProducer = 101, kErrTcMma = 102, kErrTcEpilogue = 103, kErrTcDrain = 104 };
 
+// Accumulation: the tensor core's FP32 accumulator is exact for each
+// product but not correctly rounded when many products are summed, so the
+// k loop is cut into chunks of kTcChunk k-blocks, each accumulated in its
+// own TMEM buffer (two buffers, so the MMA warp runs one chunk ahead) and
+// added by the epilogue warps into a per-thread FP32 register row.
 template <int BN, int P, int STAGES>
 __global__ void __launch_bounds__(kTcThreads, 1)
     gemm_split_bf16_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
@@ -65,22 +76,27 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint8_t* tiles = smem;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * Cfg::STAGE);
   uint64_t* empty = full + STAGES;
-  uint64_t* accb = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+  uint64_t* tfull = empty + STAGES;  // [2] chunk accumulator ready
+  uint64_t* tempty = tfull + 2;      // [2] chunk accumulator drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kTcBM, n0 = blockIdx.x * BN;
+  const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(accb, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+    }
     tc::fence_mbar_init();
   }
   if (warp == 1) {
-    tc::tmem_alloc(tmem_slot, BN);
+    tc::tmem_alloc(tmem_slot, Cfg::TMEM_COLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -120,55 +136,80 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, BN);
       bool ok = true;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!tc::mbar_wait(&full[s], ph)) {
+      for (int c = 0; c < nchunks && ok; ++c) {
+        const int b = c & 1;
+        if (!tc::mbar_wait(&tempty[b], ((c >> 1) & 1) ^ 1)) {
           atomicExch(err, kErrTcMma);
           ok = false;
           break;
         }
         tc::tc_fence_after();
-        const uint8_t* st = tiles + s * Cfg::STAGE;
+        const uint32_t acc = tmem + uint32_t(b * BN);
+        const int kb1 = min(nk, (c + 1) * kTcChunk);
+        for (int kb = c * kTcChunk; kb < kb1; ++kb) {
+          const int s = kb % STAGES;
+          const uint32_t ph = (kb / STAGES) & 1;
+          if (!tc::mbar_wait(&full[s], ph)) {
+            atomicExch(err, kErrTcMma);
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint8_t* st = tiles + s * Cfg::STAGE;
 #pragma unroll
-        for (int q = 0; q < Cfg::NPAIRS; ++q) {
-          int pa, pb;
-          term_pair(P, q, pa, pb);
-          const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
-          const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+          for (int q = 0; q < Cfg::NPAIRS; ++q) {
+            int pa, pb;
+            term_pair(q, pa, pb);
+            const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+            const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
 #pragma unroll
-          for (int j = 0; j < kTcBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
-            tc::mma_bf16(tmem, ad + 2 * j, bd + 2 * j, idesc, (kb | q | j) != 0);
+            for (int j = 0; j < kTcBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
+              tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+          }
+          tc::mma_commit(&empty[s]);
         }
-        tc::mma_commit(&empty[s]);
+        if (ok) tc::mma_commit(&tfull[b]);
       }
-      if (ok) tc::mma_commit(accb);
     }
   } else {
-    // epilogue warps 2..5: warp w reads TMEM lanes [32*(w%4), 32*(w%4)+32)
+    // epilogue warps 2..5: warp w owns TMEM lanes [32*(w%4), 32*(w%4)+32),
+    // i.e. one output row per thread, all BN columns in registers
     const int q = warp & 3;
     const int row = q * 32 + lane;
     const int gm = m0 + row;
-    const bool ok = tc::mbar_wait(accb, 0);
-    if (!ok && lane == 0) atomicExch(err, kErrTcEpilogue);
-    tc::tc_fence_after();
-    if (ok) {
-#pragma unroll 1
+    float sum[BN];
+#pragma unroll
+    for (int i = 0; i < BN; ++i) sum[i] = 0.f;
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+      const int b = c & 1;
+      if (!tc::mbar_wait(&tfull[b], (c >> 1) & 1)) {
+        if (lane == 0) atomicExch(err, kErrTcEpilogue);
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+#pragma unroll
       for (int c0 = 0; c0 < BN; c0 += 32) {
         uint32_t r[32];
-        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(c0), r);
+        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * BN + c0), r);
         tc::tmem_ld_wait();
-        if (gm < M) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const int gn = n0 + c0 + i;
-            if (gn < N) {
-              float* cp = C + int64_t(gm) + int64_t(gn) * ldc;
-              float v = alpha * __uint_as_float(r[i]);
-              if (beta != 0.f) v = fmaf(beta, *cp, v);
-              *cp = v;
-            }
-          }
+        for (int i = 0; i < 32; ++i) sum[c0 + i] += __uint_as_float(r[i]);
+      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty[b]);
+    }
+    if (ok && gm < M) {
+#pragma unroll
+      for (int i = 0; i < BN; ++i) {
+        const int gn = n0 + i;
+        if (gn < N) {
+          float* cp = C + int64_t(gm) + int64_t(gn) * ldc;
+          float v = alpha * sum[i];
+          if (beta != 0.f) v = fmaf(beta, *cp, v);
+          *cp = v;
         }
       }
     }
@@ -177,7 +218,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   if (warp == 1) {
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, BN);
+    tc::tmem_dealloc(tmem, Cfg::TMEM_COLS);
   }
 }
 
@@ -227,7 +268,7 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-static EncodeTiledFn encode_fn() {
+EncodeTiledFn tensor_map_encoder() {
   static EncodeTiledFn fn = nullptr;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -243,7 +284,7 @@ static EncodeTiledFn encode_fn() {
 
 // [P][rows][Kp] BF16 terms, box = 64 (k) x box_rows x 1
 static gbblas_status_t make_term_map(CUtensorMap* map, void* base, int64_t rows, int64_t Kp, int P, int box_rows) {
-  EncodeTiledFn fn = encode_fn();
+  EncodeTiledFn fn = tensor_map_encoder();
   if (!fn) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[3] = {cuuint64_t(Kp), cuuint64_t(rows), cuuint64_t(P)};
   cuuint64_t strides[2] = {cuuint64_t(Kp * 2), cuuint64_t(rows * Kp * 2)};
@@ -295,8 +336,8 @@ static gbblas_status_t split_gemm_one(gbblas_handle_t h, const GemmArgs<float>& 
   // A(m, k): (ta ? A[k + m*lda] : A[m + k*lda]);  B as rows n: (tb ? B[n + k*ldb] : B[k + n*ldb])
   GB_TRY(launch_split<P>(h, A, g.ta ? g.lda : 1, g.ta ? 1 : g.lda, M, K, Kp, at));
   GB_TRY(launch_split<P>(h, B, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, K, Kp, bt));
-  constexpr int BN = P == 3 ? 128 : 256;
-  constexpr int STAGES = P == 1 ? 4 : 2;
+  constexpr int BN = 128;
+  constexpr int STAGES = P == 3 ? 2 : (P == 2 ? 3 : 6);
   CUtensorMap ma, mb;
   GB_TRY(make_term_map(&ma, at, M, Kp, P, kTcBM));
   GB_TRY(make_term_map(&mb, bt, N, Kp, P, BN));

@@ -7,7 +7,7 @@
 // each output tile; the alpha/beta epilogue is fused.  beta == 0 never reads
 // y (blas2_interface.hpp:205-211); trans 'n'/'N' is the normal sweep and any
 // other character the transposed one (blas2_interface.hpp:1163-1192).
-#include "matvec.cuh"
+#include "stream_sweep.cuh"
 
 namespace gb {
 
@@ -45,6 +45,8 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
   constexpr int RPT = 16 / sizeof(T);
   const bool vec = (lda % RPT == 0) && aligned16(a);
   if (!tr) {
+    gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
+    if (try_rows_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;
     SweepPlan p = plan_rows(m, n, h->sm_count, sizeof(T));
     T* partials = nullptr;
     if (p.split > 1) {
@@ -60,6 +62,10 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
       rows_sweep<GemvPolicy<T>, T, false, true><<<grid, kMvThreads, 0, h->stream>>>(
           pol, m, n, a, lda, xb, incx, p.per_split, partials, h->tickets);
     return after_launch("gemv_n");
+  }
+  {
+    gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
+    if (try_cols_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;
   }
   SweepPlan p = plan_cols(m, n, h->sm_count, sizeof(T));
   const int64_t chunk_cols = int64_t(kMaxTickets) * p.cols_per_cta;

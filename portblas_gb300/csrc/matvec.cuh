@@ -42,7 +42,7 @@ constexpr int kMvWarps = kMvThreads / 32;
 // CTA = 8 warps over a block of 32*RPT rows; warp w takes columns
 // c0+w, c0+w+8, ... of its split; the 8 warp partials fold in warp order.
 template <class P, typename T, bool VEC, bool HAS_X>
-__global__ void __launch_bounds__(kMvThreads)
+__global__ void __launch_bounds__(kMvThreads, 8)
     rows_sweep(P pol, int64_t M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
                int64_t incx, int64_t cols_per_split, typename P::Acc* __restrict__ partials,
                unsigned int* __restrict__ tickets) {
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kMvThreads)
 // the chunk is staged in shared memory; warp w takes columns w, w+8, ... and
 // reads each column chunk with 128-bit loads, 4 in flight per lane.
 template <class P, typename T, bool VEC, bool HAS_X>
-__global__ void __launch_bounds__(kMvThreads)
+__global__ void __launch_bounds__(kMvThreads, 8)
     cols_sweep(P pol, int64_t M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
                int64_t incx, int64_t rows_per_split, int cols_per_cta, typename P::Acc* __restrict__ partials,
                unsigned int* __restrict__ tickets) {

@@ -19,7 +19,7 @@
 // its tests use.
 #include <cfloat>
 
-#include "matvec.cuh"
+#include "stream_sweep.cuh"
 
 namespace gb {
 
@@ -100,6 +100,9 @@ gbblas_status_t reduction_op(gbblas_handle_t h, int dim, const T* in, int64_t ld
   using Acc = typename P::Acc;
   if (dim == GBBLAS_DIM_OUTER) {
     P pol{out, cols};
+    gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
+    if (try_rows_sweep_tma<P, T, false>(h, pol, rows, cols, in, ld, static_cast<const T*>(nullptr), 0, &st))
+      return st;
     SweepPlan p = plan_rows(rows, cols, h->sm_count, sizeof(T));
     Acc* partials = nullptr;
     if (p.split > 1) {
@@ -115,6 +118,12 @@ gbblas_status_t reduction_op(gbblas_handle_t h, int dim, const T* in, int64_t ld
       rows_sweep<P, T, false, false><<<grid, kMvThreads, 0, h->stream>>>(pol, rows, cols, in, ld, nullptr, 0,
                                                                          p.per_split, partials, h->tickets);
     return after_launch("reduction_outer");
+  }
+  {
+    P pol{out, rows};
+    gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
+    if (try_cols_sweep_tma<P, T, false>(h, pol, rows, cols, in, ld, static_cast<const T*>(nullptr), 0, &st))
+      return st;
   }
   SweepPlan p = plan_cols(rows, cols, h->sm_count, sizeof(T));
   const int64_t chunk_cols = int64_t(kMaxTickets) * p.cols_per_cta;

@@ -1,0 +1,398 @@
+// stream_sweep.cuh — TMA-fed versions of the two column-major matrix sweeps
+// (see matvec.cuh for the math and the split / last-CTA combine).
+//
+// A dedicated producer warp streams 16 KB tiles of A into a ring of shared
+// memory stages with 2-D tensor-map copies (cp.async.bulk.tensor, mbarrier
+// completion); eight consumer warps fold them.  The bytes in flight per SM
+// are then set by the ring (3 CTAs x 4 stages x 16 KB), not by registers,
+// which is what keeps an HBM-bound sweep near the copy roofline.  Used when
+// lda and the base pointer meet the tensor-map alignment rules (16-byte
+// aligned base, lda * sizeof(T) a multiple of 16); the register-streaming
+// kernels of matvec.cuh handle every other layout.
+//
+// Tiles that overhang the matrix are zero-filled by the copy engine; the
+// consumers still mask rows >= M, columns outside their split and rows
+// outside their chunk, so operators other than Add (Max, Min, Product) see
+// only real elements.
+#pragma once
+
+#include "matvec.cuh"
+#include "tc_ptx.cuh"
+
+namespace gb {
+
+constexpr int kStStages = 4;
+constexpr int kStConsumers = 8;                       // consumer warps
+constexpr int kStThreads = (kStConsumers + 1) * 32;   // + one producer warp
+constexpr int kStTileBytes = 16384;
+
+enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203 };
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int32_t c0,
+                                            int32_t c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(tc::smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(tc::smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// Producer loop shared by both sweeps: tile t of `ntiles` at coordinates
+// (x0 + t*dx, y0 + t*dy).  Returns after every issued copy has landed.
+template <int BOX_BYTES>
+__device__ __forceinline__ void sweep_producer(const CUtensorMap* map, uint8_t* ring, uint64_t* full,
+                                               uint64_t* empty, int ntiles, int32_t x0, int32_t dx, int32_t y0,
+                                               int32_t dy, int* err) {
+  tc::tma_prefetch_desc(map);
+  int issued = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const int s = t % kStStages;
+    const uint32_t ph = (t / kStStages) & 1;
+    if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
+      atomicExch(err, kErrSweepEmpty);
+      break;
+    }
+    tc::mbar_arrive_expect_tx(&full[s], BOX_BYTES);
+    tma_load_2d(ring + s * kStTileBytes, map, &full[s], x0 + t * dx, y0 + t * dy);
+    issued = t + 1;
+  }
+  for (int t = issued > kStStages ? issued - kStStages : 0; t < issued; ++t)
+    if (!tc::mbar_wait(&full[t % kStStages], (t / kStStages) & 1)) {
+      atomicExch(err, kErrSweepDrain);
+      break;
+    }
+}
+
+// ------------------------------------------------------------ rows sweep --
+// CTA: BM rows (512 bytes) x one column split; tile = BM x 32 columns.
+// Consumer warp w folds columns w, w+8, w+16, w+24 of each tile; lane l owns
+// rows l*RPT .. l*RPT+RPT-1 (one 128-bit shared load per column).
+template <class P, typename T, bool HAS_X>
+__global__ void __launch_bounds__(kStThreads)
+    rows_sweep_tma(const __grid_constant__ CUtensorMap tmA, P pol, int64_t M, int64_t N, const T* __restrict__ xb,
+                   int64_t incx, int64_t cols_per_split, typename P::Acc* __restrict__ partials,
+                   unsigned int* __restrict__ tickets, int* __restrict__ err) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  constexpr int BM = 32 * RPT;
+  constexpr int BC = kStTileBytes / (BM * int(sizeof(T)));  // 32
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
+  uint64_t* empty = full + kStStages;
+  Acc* red = reinterpret_cast<Acc*>(empty + kStStages);  // [kStConsumers][BM]
+  __shared__ bool is_last;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rblock = blockIdx.x;
+  const int64_t r0 = rblock * BM;
+  const int64_t c0 = int64_t(blockIdx.y) * cols_per_split;
+  const int64_t c1 = min(N, c0 + cols_per_split);
+  const int ntiles = int(cdiv(c1 - c0, BC));
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], kStConsumers);
+    }
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+
+  if (warp == kStConsumers) {
+    if (lane == 0)
+      sweep_producer<kStTileBytes>(&tmA, ring, full, empty, ntiles, int32_t(r0), 0, int32_t(c0), BC, err);
+  } else {
+    Acc acc[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
+    for (int t = 0; t < ntiles; ++t) {
+      const int s = t % kStStages;
+      if (!tc::mbar_wait(&full[s], (t / kStStages) & 1)) {
+        if (lane == 0) atomicExch(err, kErrSweepFull);
+        break;
+      }
+      const T* tile = reinterpret_cast<const T*>(ring + s * kStTileBytes);
+      const int64_t cbase = c0 + int64_t(t) * BC;
+#pragma unroll
+      for (int u = 0; u < BC / kStConsumers; ++u) {
+        const int jj = warp + u * kStConsumers;
+        const int64_t gc = cbase + jj;
+        if (gc < c1) {
+          T v[RPT];
+          Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(tile + jj * BM + lane * RPT), v);
+          const T xv = HAS_X ? xb[gc * incx] : T(1);
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[r], xv);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&empty[s]);
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) red[warp * BM + lane * RPT + r] = acc[r];
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int64_t row = r0 + t;
+  Acc sacc;
+  if (t < BM) {
+    sacc = red[t];
+#pragma unroll
+    for (int w = 1; w < kStConsumers; ++w) pol.merge(sacc, red[w * BM + t]);
+  }
+  if (gridDim.y == 1) {
+    if (t < BM && row < M) pol.finish(sacc, row);
+    return;
+  }
+  if (t < BM && row < M) partials[int64_t(blockIdx.y) * M + row] = sacc;
+  __threadfence();
+  __syncthreads();
+  if (t == 0) is_last = atomicAdd(tickets + rblock, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (t < BM && row < M) {
+    Acc f = ldcg_any(partials + row);
+    for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * M + row));
+    pol.finish(f, row);
+  }
+  if (t == 0) tickets[rblock] = 0u;
+}
+
+// ------------------------------------------------------------ cols sweep --
+// CTA: 16 columns x one chunk of rows; tile = BR rows (1 KB) x 16 columns.
+// Consumer warp w folds columns 2w and 2w+1 of the tile; lane l reads rows
+// l*RPT + {0, 32*RPT} (two 128-bit shared loads per column) and the matching
+// x from the chunk's copy of x in shared memory.
+template <class P, typename T, bool HAS_X>
+__global__ void __launch_bounds__(kStThreads)
+    cols_sweep_tma(const __grid_constant__ CUtensorMap tmA, P pol, int64_t M, int64_t N, const T* __restrict__ xb,
+                   int64_t incx, int64_t rows_per_split, typename P::Acc* __restrict__ partials,
+                   unsigned int* __restrict__ tickets, int* __restrict__ err) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  constexpr int BR = 64 * RPT;                                  // 1 KB of rows
+  constexpr int BC = kStTileBytes / (BR * int(sizeof(T)));      // 16 columns
+  constexpr int CPW = BC / kStConsumers;                        // 2 columns per warp
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
+  uint64_t* empty = full + kStStages;
+  T* xs = reinterpret_cast<T*>(empty + kStStages);  // [rows_per_split]
+  __shared__ Acc colres[BC];
+  __shared__ bool is_last;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t cb = int64_t(blockIdx.x) * BC;
+  const int64_t r0 = int64_t(blockIdx.y) * rows_per_split;
+  const int64_t rlen = min(M - r0, rows_per_split);
+  const int ntiles = int(cdiv(rlen, BR));
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], kStConsumers);
+    }
+    tc::fence_mbar_init();
+  }
+  if (HAS_X)
+    for (int64_t i = threadIdx.x; i < int64_t(ntiles) * BR; i += blockDim.x) xs[i] = i < rlen ? xb[(r0 + i) * incx] : T(0);
+  __syncthreads();
+
+  if (warp == kStConsumers) {
+    if (lane == 0)
+      sweep_producer<kStTileBytes>(&tmA, ring, full, empty, ntiles, int32_t(r0), BR, int32_t(cb), 0, err);
+  } else {
+    Acc acc[CPW];
+#pragma unroll
+    for (int c = 0; c < CPW; ++c) acc[c] = pol.init();
+    for (int t = 0; t < ntiles; ++t) {
+      const int s = t % kStStages;
+      if (!tc::mbar_wait(&full[s], (t / kStStages) & 1)) {
+        if (lane == 0) atomicExch(err, kErrSweepFull);
+        break;
+      }
+      const T* tile = reinterpret_cast<const T*>(ring + s * kStTileBytes);
+      const int64_t rt = int64_t(t) * BR;  // row offset within the chunk
+      const bool full_tile = rt + BR <= rlen;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int rr = lane * RPT + h * 32 * RPT;
+        T xv[RPT];
+        if (HAS_X) Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(xs + rt + rr), xv);
+#pragma unroll
+        for (int c = 0; c < CPW; ++c) {
+          const int jj = warp * CPW + c;
+          T v[RPT];
+          Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(tile + jj * BR + rr), v);
+#pragma unroll
+          for (int e = 0; e < RPT; ++e)
+            if (full_tile || rt + rr + e < rlen) pol.add(acc[c], v[e], HAS_X ? xv[e] : T(1));
+        }
+      }
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&empty[s]);
+    }
+#pragma unroll
+    for (int c = 0; c < CPW; ++c) {
+      Acc a = acc[c];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) pol.merge(a, pol.shfl_down(a, off));
+      if (lane == 0) colres[warp * CPW + c] = a;
+    }
+  }
+  __syncthreads();
+  const int tt = threadIdx.x;
+  if (gridDim.y == 1) {
+    if (tt < BC && cb + tt < N) pol.finish(colres[tt], cb + tt);
+    return;
+  }
+  if (tt < BC && cb + tt < N) partials[int64_t(blockIdx.y) * N + cb + tt] = colres[tt];
+  __threadfence();
+  __syncthreads();
+  if (tt == 0) is_last = atomicAdd(tickets + blockIdx.x, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (tt < BC && cb + tt < N) {
+    Acc f = ldcg_any(partials + cb + tt);
+    for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + cb + tt));
+    pol.finish(f, cb + tt);
+  }
+  if (tt == 0) tickets[blockIdx.x] = 0u;
+}
+
+// ------------------------------------------------------------------ host --
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder();  // gemm_tc.cu
+
+// Column-major M x N matrix, box = box_rows x box_cols, no swizzle.
+template <typename T>
+inline bool make_matrix_map(CUtensorMap* map, const T* base, int64_t M, int64_t N, int64_t lda, int box_rows,
+                            int box_cols) {
+  EncodeTiledFn fn = tensor_map_encoder();
+  if (!fn) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((lda * int64_t(sizeof(T))) & 15)) return false;
+  if (M <= 0 || N <= 0 || M > (int64_t(1) << 31) || N > (int64_t(1) << 31)) return false;
+  cuuint64_t dims[2] = {cuuint64_t(M), cuuint64_t(N)};
+  cuuint64_t strides[1] = {cuuint64_t(lda * int64_t(sizeof(T)))};
+  cuuint32_t box[2] = {cuuint32_t(box_rows), cuuint32_t(box_cols)};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
+                  const_cast<T*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Smem bytes of the two sweeps (ring + barriers + per-kernel extras + align slack).
+template <typename Acc, typename T>
+constexpr size_t rows_tma_smem() {
+  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + sizeof(Acc) * kStConsumers * 32 * (16 / sizeof(T));
+}
+template <typename T>
+inline size_t cols_tma_smem(int64_t rows_per_split) {
+  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + sizeof(T) * size_t(rows_per_split);
+}
+
+struct TmaPlan {
+  int64_t tiles, split, per_split;
+};
+
+// rows sweep: 3 resident CTAs per SM
+inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes) {
+  const int64_t BM = 512 / elem_bytes, BC = kStTileBytes / 512;
+  TmaPlan p;
+  p.tiles = cdiv(M, BM);
+  // fill the 3 resident CTAs per SM in one wave
+  int64_t split = (int64_t(sm_count) * 3) / p.tiles;
+  const int64_t max_split = cdiv(N, 4 * BC);  // at least 4 tiles per CTA
+  if (split > max_split) split = max_split;
+  if (split < 1 || p.tiles > int64_t(kMaxTickets)) split = 1;
+  p.per_split = cdiv(cdiv(N, split), BC) * BC;
+  p.split = cdiv(N, p.per_split);
+  return p;
+}
+
+// cols sweep: chunks of rows (multiple of the 1 KB tile), at most 4096 rows
+inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes) {
+  const int64_t BR = 1024 / elem_bytes, BC = kStTileBytes / 1024;
+  TmaPlan p;
+  p.tiles = cdiv(N, BC);
+  int64_t split = (int64_t(sm_count) * 3) / p.tiles;
+  const int64_t max_rows = 4096;
+  const int64_t min_split = cdiv(M, max_rows);
+  const int64_t max_split = cdiv(M, 4 * BR);
+  if (split > max_split) split = max_split;
+  if (split < min_split) split = min_split;
+  if (split < 1) split = 1;
+  p.per_split = cdiv(cdiv(M, split), BR) * BR;
+  p.split = cdiv(M, p.per_split);
+  return p;
+}
+
+// Launches the TMA rows sweep; returns false (nothing launched) when the
+// layout does not qualify.
+template <class P, typename T, bool HAS_X>
+inline bool try_rows_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64_t N, const T* A, int64_t lda,
+                               const T* xb, int64_t incx, gbblas_status_t* st) {
+  using Acc = typename P::Acc;
+  constexpr int BM = 512 / int(sizeof(T));
+  constexpr int BC = kStTileBytes / 512;
+  if (M < BM || N < 4 * BC) return false;
+  TmaPlan p = plan_rows_tma(M, N, h->sm_count, sizeof(T));
+  if (p.split > 65535 || p.tiles > INT32_MAX) return false;
+  CUtensorMap map;
+  if (!make_matrix_map(&map, A, M, N, lda, BM, BC)) return false;
+  Acc* partials = nullptr;
+  if (p.split > 1) {
+    void* tmp;
+    *st = temp_acquire(h, sizeof(Acc) * p.split * M, &tmp);
+    if (*st != GBBLAS_STATUS_SUCCESS) return true;
+    partials = static_cast<Acc*>(tmp);
+  }
+  constexpr size_t smem = rows_tma_smem<Acc, T>();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(rows_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    attr = true;
+  }
+  dim3 grid(unsigned(p.tiles), unsigned(p.split));
+  rows_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(map, pol, M, N, xb, incx, p.per_split,
+                                                                     partials, h->tickets, h->dev_error);
+  *st = after_launch("rows_sweep_tma");
+  return true;
+}
+
+template <class P, typename T, bool HAS_X>
+inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64_t N, const T* A, int64_t lda,
+                               const T* xb, int64_t incx, gbblas_status_t* st) {
+  using Acc = typename P::Acc;
+  constexpr int BR = 1024 / int(sizeof(T));
+  constexpr int BC = kStTileBytes / 1024;
+  if (M < 4 * BR || N < BC) return false;
+  TmaPlan p = plan_cols_tma(M, N, h->sm_count, sizeof(T));
+  if (p.split > 65535 || p.tiles > int64_t(kMaxTickets)) return false;
+  CUtensorMap map;
+  if (!make_matrix_map(&map, A, M, N, lda, BR, BC)) return false;
+  Acc* partials = nullptr;
+  if (p.split > 1) {
+    void* tmp;
+    *st = temp_acquire(h, sizeof(Acc) * p.split * N, &tmp);
+    if (*st != GBBLAS_STATUS_SUCCESS) return true;
+    partials = static_cast<Acc*>(tmp);
+  }
+  const size_t smem = cols_tma_smem<T>(p.per_split);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(cols_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(cols_tma_smem<T>(4096)));
+    attr = true;
+  }
+  dim3 grid(unsigned(p.tiles), unsigned(p.split));
+  cols_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(map, pol, M, N, xb, incx, p.per_split,
+                                                                     partials, h->tickets, h->dev_error);
+  *st = after_launch("cols_sweep_tma");
+  return true;
+}
+
+}  // namespace gb

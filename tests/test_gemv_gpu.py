@@ -76,3 +76,30 @@ def test_gemv_full_size_linearity(sb, torch_cuda, trans):
     ref = (A @ x1.double()) if trans == "n" else (A.T @ x1.double())
     err = (ys[0].double() - ref).abs().max().item()
     assert err <= 2e-5 * ref.abs().max().item() * 8
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+@pytest.mark.parametrize("m,n,lda", [(1000, 700, 1000), (4100, 300, 4104), (520, 1030, 520), (8192, 257, 8192),
+                                     (257, 5000, 260)])
+@pytest.mark.parametrize("beta", [0.0, 0.5])
+def test_gemv_tma_stream_path(sb, torch_cuda, trans, m, n, lda, beta):
+    """Shapes whose lda satisfies the tensor-map rules take the TMA-fed sweeps:
+    ragged row/column tiles, split combines, strided x/y."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(m + n + lda)
+    a = g.uniform(-1, 1, lda * n).astype(np.float32)
+    xlen, ylen = (n, m) if trans == "n" else (m, n)
+    x = g.uniform(-1, 1, xlen * 2).astype(np.float32)
+    y = g.uniform(-1, 1, ylen * 3).astype(np.float32)
+    ref = oracle.gemv(trans, m, n, 1.25, a, lda, x, 2, beta, y, 3)
+    yd = to_dev(y, torch)
+    blas._gemv(sb, trans, m, n, 1.25, to_dev(a, torch), lda, to_dev(x, torch), 2, beta, yd, 3)
+    got = oracle.view(to_host(yd), ylen, 3)
+    assert_almost_equal(got, ref)
+    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=2e-5 * np.abs(ref).max())
+    # entries of y between the strided elements are untouched
+    yo = to_host(yd)
+    mask = np.ones(len(y), bool)
+    mask[: ylen * 3: 3] = False
+    np.testing.assert_array_equal(yo[mask], y[mask])

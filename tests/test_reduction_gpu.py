@@ -96,3 +96,25 @@ def test_reduction_full_size(sb, torch_cuda, dim):
     ref = A.double().sum(1) if dim == "inner" else A.double().sum(0)
     err = (out.double() - ref).abs().max().item()
     assert err <= 1e-5 * 128
+
+
+@pytest.mark.parametrize("op", OPS)
+@pytest.mark.parametrize("dim", ["inner", "outer"])
+@pytest.mark.parametrize("rows,cols,ld", [(1000, 700, 1000), (4100, 300, 4104), (520, 1030, 520),
+                                          (130, 5000, 132), (9000, 64, 9000)])
+def test_reduction_tma_stream_path(sb, torch_cuda, op, dim, rows, cols, ld):
+    """Shapes whose ld satisfies the tensor-map rules take the TMA-fed sweeps;
+    ragged tiles must not leak zero fill into Max / Min / Product."""
+    g = rng(rows * 3 + cols + ld)
+    lo, hi = (0.995, 1.005) if op == "product" else (-5.0, -1.0)  # all-negative data catches a zero leak in Max
+    if op == "min":
+        lo, hi = 1.0, 5.0  # all-positive data catches a zero leak in Min
+    data = g.uniform(lo, hi, ld * cols).astype(np.float32)
+    ref = oracle.reduction(op, dim, data, ld, rows, cols)
+    got = _run(sb, torch_cuda, op, dim, data, ld, rows, cols)
+    if op in ("max", "min"):
+        np.testing.assert_array_equal(got, ref.astype(np.float32))
+    elif op == "product":
+        np.testing.assert_allclose(got, ref, rtol=1e-3)
+    else:
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
