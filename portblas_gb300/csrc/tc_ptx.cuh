@@ -45,12 +45,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: gives up after `limit` polls (each poll may suspend for a
-// hardware-chosen interval) and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 26)) {
-  for (uint32_t i = 0; i < limit; ++i)
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: polls until the phase completes or about `limit_ns` of wall
+// time (default 2 s) has passed, then returns false.  Healthy waits finish
+// in microseconds; the bound only turns a defect into an error code instead
+// of a hung GPU.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = 2000000000ull) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-  return false;
+    if ((i & 63) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
+  }
 }
 
 // ---------------------------------------------------------------------- TMA --
