@@ -297,7 +297,15 @@ class extension:
 
 
 # --------------------------------------------------------- grouped GEMM --
-_DTYPE_CODES = {"float32": 0, "bfloat16": 1, "torch.float32": 0, "torch.bfloat16": 1}
+_DTYPE_CODES = {"float32": 0, "bfloat16": 1, "float64": 2, "torch.float32": 0, "torch.bfloat16": 1,
+                "torch.float64": 2}
+
+
+def _dtype_code(dtype) -> int:
+    try:
+        return _DTYPE_CODES[str(dtype)]
+    except KeyError:
+        raise UnsupportedException(f"grouped GEMM: element type {dtype} is not supported") from None
 
 
 def _grouped_arrays(problems):
@@ -326,7 +334,7 @@ def _gemm_grouped(sb_handle, problems, dtype="float32"):
     transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc (a/b/c CUDA tensors or
     addresses); A and B are ``dtype`` (float32 or bfloat16), C is float32."""
     args, keep = _grouped_arrays(problems)
-    return _call("gbblas_gemm_grouped", sb_handle.handle, _DTYPE_CODES[str(dtype)], *args)
+    return _call("gbblas_gemm_grouped", sb_handle.handle, _dtype_code(dtype), *args)
 
 
 class GroupedPlan:
@@ -338,7 +346,7 @@ class GroupedPlan:
         self.sb = sb_handle
         args, self._keep = _grouped_arrays(problems)
         p = C.c_void_p()
-        _check(self._L.gbblas_grouped_plan_create(sb_handle.handle, _DTYPE_CODES[str(dtype)], *args, C.byref(p)))
+        _check(self._L.gbblas_grouped_plan_create(sb_handle.handle, _dtype_code(dtype), *args, C.byref(p)))
         self._p = p
 
     def run(self):

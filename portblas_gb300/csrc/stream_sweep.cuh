@@ -28,6 +28,12 @@ constexpr int kStTileBytes = 16384;
 
 enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203 };
 
+// x elements staged in shared memory by the rows sweep (one column split)
+constexpr int64_t kRowsXStage = 8192;
+
+// barrier among the 8 consumer warps only (the producer keeps streaming)
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int32_t c0,
                                             int32_t c1) {
   asm volatile(
@@ -80,6 +86,7 @@ __global__ void __launch_bounds__(kStThreads)
   uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
   uint64_t* empty = full + kStStages;
   Acc* red = reinterpret_cast<Acc*>(empty + kStStages);  // [kStConsumers][BM]
+  T* xs = reinterpret_cast<T*>(red + kStConsumers * BM);  // [cols_per_split] when staged
   __shared__ bool is_last;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -101,6 +108,12 @@ __global__ void __launch_bounds__(kStThreads)
     if (lane == 0)
       sweep_producer<kStTileBytes>(&tmA, ring, full, empty, ntiles, int32_t(r0), 0, int32_t(c0), BC, err);
   } else {
+    // x of this column split goes to shared memory while the first tiles land
+    const bool xstaged = HAS_X && cols_per_split <= kRowsXStage;
+    if (xstaged) {
+      for (int64_t i = threadIdx.x; i < c1 - c0; i += kStConsumers * 32) xs[i] = xb[(c0 + i) * incx];
+      consumers_sync();
+    }
     Acc acc[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
@@ -119,7 +132,7 @@ __global__ void __launch_bounds__(kStThreads)
         if (gc < c1) {
           T v[RPT];
           Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(tile + jj * BM + lane * RPT), v);
-          const T xv = HAS_X ? xb[gc * incx] : T(1);
+          const T xv = HAS_X ? (xstaged ? xs[gc - c0] : xb[gc * incx]) : T(1);
 #pragma unroll
           for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[r], xv);
         }
@@ -159,14 +172,16 @@ __global__ void __launch_bounds__(kStThreads)
 }
 
 // ------------------------------------------------------------ cols sweep --
-// CTA: 16 columns x one chunk of rows; tile = BR rows (1 KB) x 16 columns.
-// Consumer warp w folds columns 2w and 2w+1 of the tile; lane l reads rows
-// l*RPT + {0, 32*RPT} (two 128-bit shared loads per column) and the matching
-// x from the chunk's copy of x in shared memory.
+// CTA: `ctiles` consecutive 16-column tiles x one chunk of rows; each tile is
+// BR rows (1 KB) x 16 columns and the producer streams the chunk's row tiles
+// of each column tile in turn.  Consumer warp w folds columns 2w and 2w+1 of
+// a tile; lane l reads rows l*RPT + {0, 32*RPT} (two 128-bit shared loads
+// per column) and the matching x from the chunk's copy of x in shared memory
+// (staged once per CTA while the first tiles land).
 template <class P, typename T, bool HAS_X>
 __global__ void __launch_bounds__(kStThreads)
     cols_sweep_tma(const __grid_constant__ CUtensorMap tmA, P pol, int64_t M, int64_t N, const T* __restrict__ xb,
-                   int64_t incx, int64_t rows_per_split, typename P::Acc* __restrict__ partials,
+                   int64_t incx, int64_t rows_per_split, int ctiles, typename P::Acc* __restrict__ partials,
                    unsigned int* __restrict__ tickets, int* __restrict__ err) {
   using Acc = typename P::Acc;
   constexpr int RPT = Pack16<T>::n;
@@ -177,15 +192,15 @@ __global__ void __launch_bounds__(kStThreads)
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
   uint64_t* empty = full + kStStages;
-  T* xs = reinterpret_cast<T*>(empty + kStStages);  // [rows_per_split]
-  __shared__ Acc colres[BC];
+  T* xs = reinterpret_cast<T*>(empty + kStStages);  // [rows_per_split] when HAS_X
   __shared__ bool is_last;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t cb = int64_t(blockIdx.x) * BC;
+  const int64_t ct0 = int64_t(blockIdx.x) * ctiles;          // first column tile of this CTA
+  const int nct = int(min(int64_t(ctiles), cdiv(N, BC) - ct0));
   const int64_t r0 = int64_t(blockIdx.y) * rows_per_split;
   const int64_t rlen = min(M - r0, rows_per_split);
-  const int ntiles = int(cdiv(rlen, BR));
+  const int nrt = int(cdiv(rlen, BR));  // row tiles per column tile
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStStages; ++s) {
       tc::mbar_init(&full[s], 1);
@@ -193,71 +208,105 @@ __global__ void __launch_bounds__(kStThreads)
     }
     tc::fence_mbar_init();
   }
-  if (HAS_X)
-    for (int64_t i = threadIdx.x; i < int64_t(ntiles) * BR; i += blockDim.x) xs[i] = i < rlen ? xb[(r0 + i) * incx] : T(0);
   __syncthreads();
 
   if (warp == kStConsumers) {
-    if (lane == 0)
-      sweep_producer<kStTileBytes>(&tmA, ring, full, empty, ntiles, int32_t(r0), BR, int32_t(cb), 0, err);
-  } else {
-    Acc acc[CPW];
-#pragma unroll
-    for (int c = 0; c < CPW; ++c) acc[c] = pol.init();
-    for (int t = 0; t < ntiles; ++t) {
-      const int s = t % kStStages;
-      if (!tc::mbar_wait(&full[s], (t / kStStages) & 1)) {
-        if (lane == 0) atomicExch(err, kErrSweepFull);
-        break;
+    if (lane == 0) {
+      // tile t: column tile t / nrt, row tile t % nrt
+      tc::tma_prefetch_desc(&tmA);
+      const int ntiles = nct * nrt;
+      int issued = 0;
+      for (int t = 0; t < ntiles; ++t) {
+        const int s = t % kStStages;
+        if (!tc::mbar_wait(&empty[s], ((t / kStStages) & 1) ^ 1)) {
+          atomicExch(err, kErrSweepEmpty);
+          break;
+        }
+        tc::mbar_arrive_expect_tx(&full[s], kStTileBytes);
+        tma_load_2d(ring + s * kStTileBytes, &tmA, &full[s], int32_t(r0 + int64_t(t % nrt) * BR),
+                    int32_t((ct0 + t / nrt) * BC));
+        issued = t + 1;
       }
-      const T* tile = reinterpret_cast<const T*>(ring + s * kStTileBytes);
-      const int64_t rt = int64_t(t) * BR;  // row offset within the chunk
-      const bool full_tile = rt + BR <= rlen;
+      for (int t = issued > kStStages ? issued - kStStages : 0; t < issued; ++t)
+        if (!tc::mbar_wait(&full[t % kStStages], (t / kStStages) & 1)) {
+          atomicExch(err, kErrSweepDrain);
+          break;
+        }
+    }
+  } else {
+    if (HAS_X) {
+      for (int64_t i = threadIdx.x; i < int64_t(nrt) * BR; i += kStConsumers * 32)
+        xs[i] = i < rlen ? xb[(r0 + i) * incx] : T(0);
+      consumers_sync();
+    }
+    bool ok = true;
+    for (int c = 0; c < nct && ok; ++c) {
+      Acc acc[CPW];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int rr = lane * RPT + h * 32 * RPT;
-        T xv[RPT];
-        if (HAS_X) Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(xs + rt + rr), xv);
+      for (int q = 0; q < CPW; ++q) acc[q] = pol.init();
+      for (int rt = 0; rt < nrt; ++rt) {
+        const int t = c * nrt + rt;
+        const int s = t % kStStages;
+        if (!tc::mbar_wait(&full[s], (t / kStStages) & 1)) {
+          if (lane == 0) atomicExch(err, kErrSweepFull);
+          ok = false;
+          break;
+        }
+        const T* tile = reinterpret_cast<const T*>(ring + s * kStTileBytes);
+        const int64_t roff = int64_t(rt) * BR;  // row offset within the chunk
+        const bool full_tile = roff + BR <= rlen;
 #pragma unroll
-        for (int c = 0; c < CPW; ++c) {
-          const int jj = warp * CPW + c;
-          T v[RPT];
-          Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(tile + jj * BR + rr), v);
+        for (int h = 0; h < 2; ++h) {
+          const int rr = lane * RPT + h * 32 * RPT;
+          T xv[RPT];
+          if (HAS_X) Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(xs + roff + rr), xv);
 #pragma unroll
-          for (int e = 0; e < RPT; ++e)
-            if (full_tile || rt + rr + e < rlen) pol.add(acc[c], v[e], HAS_X ? xv[e] : T(1));
+          for (int q = 0; q < CPW; ++q) {
+            const int jj = warp * CPW + q;
+            T v[RPT];
+            Pack16<T>::get(*reinterpret_cast<const typename Pack16<T>::V*>(tile + jj * BR + rr), v);
+#pragma unroll
+            for (int e = 0; e < RPT; ++e)
+              if (full_tile || roff + rr + e < rlen) pol.add(acc[q], v[e], HAS_X ? xv[e] : T(1));
+          }
+        }
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&empty[s]);
+      }
+      if (!ok) break;
+#pragma unroll
+      for (int q = 0; q < CPW; ++q) {
+        Acc a = acc[q];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) pol.merge(a, pol.shfl_down(a, off));
+        const int64_t col = (ct0 + c) * BC + warp * CPW + q;
+        if (lane == 0 && col < N) {
+          if (gridDim.y == 1) pol.finish(a, col);
+          else partials[int64_t(blockIdx.y) * N + col] = a;
         }
       }
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&empty[s]);
-    }
-#pragma unroll
-    for (int c = 0; c < CPW; ++c) {
-      Acc a = acc[c];
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) pol.merge(a, pol.shfl_down(a, off));
-      if (lane == 0) colres[warp * CPW + c] = a;
     }
   }
-  __syncthreads();
-  const int tt = threadIdx.x;
-  if (gridDim.y == 1) {
-    if (tt < BC && cb + tt < N) pol.finish(colres[tt], cb + tt);
-    return;
-  }
-  if (tt < BC && cb + tt < N) partials[int64_t(blockIdx.y) * N + cb + tt] = colres[tt];
+  if (gridDim.y == 1) return;
   __threadfence();
   __syncthreads();
-  if (tt == 0) is_last = atomicAdd(tickets + blockIdx.x, 1u) == gridDim.y - 1;
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  if (tt < BC && cb + tt < N) {
-    Acc f = ldcg_any(partials + cb + tt);
-    for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + cb + tt));
-    pol.finish(f, cb + tt);
+  // last CTA (over the row chunks) of each column tile folds its 16 columns
+  for (int c = 0; c < nct; ++c) {
+    const int64_t ct = ct0 + c;
+    if (threadIdx.x == 0) is_last = atomicAdd(tickets + ct, 1u) == gridDim.y - 1;
+    __syncthreads();
+    if (is_last) {
+      __threadfence();
+      const int64_t col = ct * BC + threadIdx.x;
+      if (threadIdx.x < BC && col < N) {
+        Acc f = ldcg_any(partials + col);
+        for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + col));
+        pol.finish(f, col);
+      }
+      if (threadIdx.x == 0) tickets[ct] = 0u;
+    }
+    __syncthreads();
   }
-  if (tt == 0) tickets[blockIdx.x] = 0u;
 }
 
 // ------------------------------------------------------------------ host --
@@ -286,16 +335,18 @@ inline bool make_matrix_map(CUtensorMap* map, const T* base, int64_t M, int64_t 
 
 // Smem bytes of the two sweeps (ring + barriers + per-kernel extras + align slack).
 template <typename Acc, typename T>
-constexpr size_t rows_tma_smem() {
-  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + sizeof(Acc) * kStConsumers * 32 * (16 / sizeof(T));
+constexpr size_t rows_tma_smem(bool has_x) {
+  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + sizeof(Acc) * kStConsumers * 32 * (16 / sizeof(T)) +
+         (has_x ? sizeof(T) * size_t(kRowsXStage) : 0);
 }
 template <typename T>
-inline size_t cols_tma_smem(int64_t rows_per_split) {
-  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + sizeof(T) * size_t(rows_per_split);
+inline size_t cols_tma_smem(bool has_x, int64_t rows_per_split) {
+  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + (has_x ? sizeof(T) * size_t(rows_per_split) : 0);
 }
 
 struct TmaPlan {
   int64_t tiles, split, per_split;
+  int ctiles;  // cols sweep: column tiles per CTA
 };
 
 // rows sweep: 3 resident CTAs per SM
@@ -313,20 +364,28 @@ inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes)
   return p;
 }
 
-// cols sweep: chunks of rows (multiple of the 1 KB tile), at most 4096 rows
-inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes) {
+// cols sweep: rows split into chunks (a multiple of the 1 KB tile; with x
+// at most 4096 rows so the chunk of x fits in shared memory), then each CTA
+// takes `ctiles` column tiles so the grid is about one wave of resident CTAs.
+inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes, bool has_x) {
   const int64_t BR = 1024 / elem_bytes, BC = kStTileBytes / 1024;
+  const int64_t slots = int64_t(sm_count) * (has_x ? 2 : 3);
   TmaPlan p;
-  p.tiles = cdiv(N, BC);
-  int64_t split = (int64_t(sm_count) * 3) / p.tiles;
-  const int64_t max_rows = 4096;
-  const int64_t min_split = cdiv(M, max_rows);
+  const int64_t coltiles = cdiv(N, BC);
+  int64_t split = slots / coltiles;
+  const int64_t min_split = has_x ? cdiv(M, 4096) : 1;
   const int64_t max_split = cdiv(M, 4 * BR);
   if (split > max_split) split = max_split;
   if (split < min_split) split = min_split;
   if (split < 1) split = 1;
   p.per_split = cdiv(cdiv(M, split), BR) * BR;
   p.split = cdiv(M, p.per_split);
+  // column tiles per CTA: enough CTAs for one wave, at least one tile each
+  int64_t ctiles = cdiv(coltiles * p.split, slots);
+  if (ctiles < 1) ctiles = 1;
+  if (ctiles > 64) ctiles = 64;
+  p.ctiles = int(ctiles);
+  p.tiles = cdiv(coltiles, ctiles);
   return p;
 }
 
@@ -350,10 +409,13 @@ inline bool try_rows_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
     if (*st != GBBLAS_STATUS_SUCCESS) return true;
     partials = static_cast<Acc*>(tmp);
   }
-  constexpr size_t smem = rows_tma_smem<Acc, T>();
+  // x staged only when the split's columns fit the stage
+  const size_t smem = rows_tma_smem<Acc, T>(false) +
+                      ((HAS_X && p.per_split <= kRowsXStage) ? sizeof(T) * size_t(p.per_split) : 0);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(rows_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaFuncSetAttribute(rows_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(rows_tma_smem<Acc, T>(HAS_X)));
     attr = true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));
@@ -370,8 +432,8 @@ inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
   constexpr int BR = 1024 / int(sizeof(T));
   constexpr int BC = kStTileBytes / 1024;
   if (M < 4 * BR || N < BC) return false;
-  TmaPlan p = plan_cols_tma(M, N, h->sm_count, sizeof(T));
-  if (p.split > 65535 || p.tiles > int64_t(kMaxTickets)) return false;
+  TmaPlan p = plan_cols_tma(M, N, h->sm_count, sizeof(T), HAS_X);
+  if (p.split > 65535 || cdiv(N, BC) > int64_t(kMaxTickets) || p.tiles > INT32_MAX) return false;
   CUtensorMap map;
   if (!make_matrix_map(&map, A, M, N, lda, BR, BC)) return false;
   Acc* partials = nullptr;
@@ -381,16 +443,16 @@ inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
     if (*st != GBBLAS_STATUS_SUCCESS) return true;
     partials = static_cast<Acc*>(tmp);
   }
-  const size_t smem = cols_tma_smem<T>(p.per_split);
+  const size_t smem = cols_tma_smem<T>(HAS_X, p.per_split);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(cols_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(cols_tma_smem<T>(4096)));
+                         int(cols_tma_smem<T>(HAS_X, 4096)));
     attr = true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));
-  cols_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(map, pol, M, N, xb, incx, p.per_split,
-                                                                     partials, h->tickets, h->dev_error);
+  cols_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(
+      map, pol, M, N, xb, incx, p.per_split, p.ctiles, partials, h->tickets, h->dev_error);
   *st = after_launch("cols_sweep_tma");
   return true;
 }
