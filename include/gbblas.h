@@ -161,6 +161,21 @@ gbblas_status_t gbblas_sgemv(gbblas_handle_t h, char trans, int64_t m, int64_t n
 gbblas_status_t gbblas_dgemv(gbblas_handle_t h, char trans, int64_t m, int64_t n, double alpha, const double* a,
                              int64_t lda, const double* x, int64_t incx, double beta, double* y, int64_t incy);
 
+/* Allocation-free GEMV.  No counterpart in portBLAS: it is gbblas_sgemv for
+ * callers that cannot allocate device memory (inside a stream capture, under
+ * an allocator that owns all device memory, in hosts that forbid allocation
+ * after start-up).  Same arguments and results as gbblas_sgemv, but it takes
+ * the cudaStream_t directly (no handle) and its scratch is a fixed 1 MiB
+ * block of file-scope device memory (plus 256 KiB of ticket counters) that
+ * every GPU loading the library holds until exit; a problem needing more is
+ * rejected with GBBLAS_STATUS_INVALID_ARG before anything runs.  The first
+ * call on a device looks the block up (cudaGetSymbolAddress): make it before
+ * any stream capture.  All calls share the block, so calls that overlap on
+ * the GPU race. */
+gbblas_status_t gbblas_sgemv_noalloc(void* stream, char trans, int64_t m, int64_t n, float alpha, const float* a,
+                                     int64_t lda, const float* x, int64_t incx, float beta, float* y,
+                                     int64_t incy);
+
 /* ---------------------------------------------------------------- BLAS-3 -- */
 /* blas::_gemm  (include/interface/blas3_interface.h:86-95;
  *   src/interface/gemm_interface.hpp:102-198).

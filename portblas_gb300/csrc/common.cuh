@@ -67,6 +67,9 @@ struct gbblas_handle_s {
   // Pinned host staging for the *_sync overloads.
   void* pinned = nullptr;
   int sgemm_mode = GBBLAS_SGEMM_AUTO;
+  // set for the allocation-free entry point: temp memory is a fixed block and
+  // a request beyond it is an error instead of a cudaMallocAsync
+  bool no_alloc = false;
   std::mutex mu;  // guards temp memory, as the portBLAS pool mutex does
 };
 

@@ -29,6 +29,10 @@ gbblas_status_t temp_acquire(gbblas_handle_t h, size_t bytes, void** ptr) {
   bytes = (bytes + 255) & ~size_t(255);
   if (bytes == 0) bytes = 256;
   if (bytes > h->temp_size) {
+    if (h->no_alloc)
+      return fail(GBBLAS_STATUS_INVALID_ARG, "problem needs " + std::to_string(bytes) +
+                                                 " bytes of scratch, above the allocation-free maximum of " +
+                                                 std::to_string(h->temp_size) + " bytes");
     size_t grow = h->temp_size * 2 > bytes ? h->temp_size * 2 : bytes;
     if (h->temp) {
       cudaError_t e = cudaFreeAsync(h->temp, h->stream);
