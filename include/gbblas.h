@@ -214,6 +214,55 @@ gbblas_status_t gbblas_dgemm_strided_batched(gbblas_handle_t h, char transa, cha
                                              double beta, double* c, int64_t ldc, int64_t stride_c,
                                              int64_t batch_size);
 
+/* FP32 GEMM tile configurations (no portBLAS counterpart: portBLAS fixes its
+ * tile at compile time from size thresholds,
+ * src/interface/blas3/backend/nvidia_gpu.hpp:116-171).  Configs 0..19 are
+ * SIMT tiles {128x128, 128x64, 64x128, 64x64} x split-K {1,2,4,8,16};
+ * 20..39 are the 3-term split-BF16 tcgen05 kernel with N tile {128, 64} x
+ * split-K {1,2,4,8,16} x raster {N, M}.  All are FP32-accurate; AUTO picks
+ * one per call (autotuned winner > learned selector > size heuristic). */
+int gbblas_sgemm_config_count(void);
+gbblas_status_t gbblas_sgemm_config_info(int config, int* method, int* tile_m, int* tile_n, int* split,
+                                         int* raster_m);
+gbblas_status_t gbblas_sgemm_strided_batched_config(gbblas_handle_t h, int config, char transa, char transb,
+                                                    int64_t m, int64_t n, int64_t k, float alpha, const float* a,
+                                                    int64_t lda, int64_t stride_a, const float* b, int64_t ldb,
+                                                    int64_t stride_b, float beta, float* c, int64_t ldc,
+                                                    int64_t stride_c, int64_t batch_size);
+/* Selector inputs: log2 M, N, K (/14), transa, transb, lda/ldb/ldc mod 16
+ * (/16), log2 batch (/10), dtype one-hot (FP32, BF16) — 11 floats. */
+gbblas_status_t gbblas_sgemm_features(int64_t m, int64_t n, int64_t k, char transa, char transb, int64_t lda,
+                                      int64_t ldb, int64_t ldc, int64_t batch, float* features);
+/* The fixed size-threshold selector alone (portBLAS-style tiers). */
+int gbblas_sgemm_heuristic_config(int64_t m, int64_t n, int64_t k, int64_t batch);
+/* Loads learned-selector weights (process-wide; default file
+ * tuning/sgemm_selector.bin beside the package, or $GBBLAS_SGEMM_SELECTOR,
+ * "off" disables), and asks the selector chain for a config. */
+gbblas_status_t gbblas_sgemm_load_selector(const char* path);
+gbblas_status_t gbblas_sgemm_selector_pick(int64_t m, int64_t n, int64_t k, char transa, char transb, int64_t lda,
+                                           int64_t ldb, int64_t ldc, int64_t batch, int* config);
+/* Exhaustive autotune of one shape: times every config (`reps` launches
+ * each) on zero-filled operands, remembers the winner for AUTO. */
+gbblas_status_t gbblas_sgemm_autotune(gbblas_handle_t h, char transa, char transb, int64_t m, int64_t n,
+                                      int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t batch, int reps,
+                                      int* best_config, float* best_ms);
+
+/* Training and inference kernels of the learned selector (no portBLAS
+ * counterpart).  Network in -> hidden x3 (GELU) -> out, FP32, parameters
+ * packed [W1 b1 W2 b2 W3 b3 W4 b4] (W row-major out x in) in device memory;
+ * x is [n][in], y / target / mask are [n][out].  loss_grad writes the
+ * gradients of the masked MSE (sum over mask / valid_count) and the loss
+ * (device scalar); adam applies one AdamW step. */
+gbblas_status_t gbblas_mlp_param_count(int in_dim, int hidden, int out_dim, int64_t* count);
+gbblas_status_t gbblas_mlp_forward(gbblas_handle_t h, int in_dim, int hidden, int out_dim, const float* params,
+                                   const float* x, int64_t n, float* y);
+gbblas_status_t gbblas_mlp_loss_grad(gbblas_handle_t h, int in_dim, int hidden, int out_dim, const float* params,
+                                     const float* x, const float* target, const float* mask, int64_t n,
+                                     float valid_count, float* grads, float* loss);
+gbblas_status_t gbblas_mlp_adam(gbblas_handle_t h, int64_t count, float* params, const float* grads, float* m,
+                                float* v, int step, float lr, float beta1, float beta2, float eps,
+                                float weight_decay);
+
 /* Grouped GEMM over `count` independent problems of uneven sizes, one
  * persistent launch with a device-side tile scheduler.  No portBLAS
  * counterpart takes uneven sizes; per problem the semantics are those of

@@ -49,13 +49,16 @@ static gbblas_status_t gemm_front(gbblas_handle_t h, char transa, char transb, i
 gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<double>& g) { return launch_gemm_simt(h, g); }
 
 gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g) {
-  int mode = h->sgemm_mode;
-  if (mode == GBBLAS_SGEMM_AUTO) mode = select_sgemm_method(h, g);
-  if (mode == GBBLAS_SGEMM_SPLIT_BF16X3 || mode == GBBLAS_SGEMM_SPLIT_BF16X6) {
-    gbblas_status_t s = launch_gemm_split_bf16(h, g, mode == GBBLAS_SGEMM_SPLIT_BF16X3 ? 2 : 3);
-    if (s != GBBLAS_STATUS_UNSUPPORTED || h->sgemm_mode != GBBLAS_SGEMM_AUTO) return s;
-    clear_error();  // AUTO falls through to SIMT for shapes the tensor path does not take
+  switch (h->sgemm_mode) {
+    case GBBLAS_SGEMM_FP32_SIMT: return launch_gemm_simt(h, g);
+    case GBBLAS_SGEMM_SPLIT_BF16X3: return launch_gemm_split_bf16(h, g, 2);
+    case GBBLAS_SGEMM_SPLIT_BF16X6: return launch_gemm_split_bf16(h, g, 3);
+    default: break;
   }
+  // AUTO: every config is FP32-accurate; the selector picks one
+  gbblas_status_t s = launch_sgemm_config(h, g, select_sgemm_config(h, g));
+  if (s != GBBLAS_STATUS_UNSUPPORTED) return s;
+  clear_error();  // a config that cannot take this shape (grid / workspace limits)
   return launch_gemm_simt(h, g);
 }
 

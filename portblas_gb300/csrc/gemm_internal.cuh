@@ -22,6 +22,9 @@ struct GemmArgs {
 
 // Plain FP32 / FP64 SIMT GEMM (CUDA cores), any transposes, strided batch.
 gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<float>& g);
+// FP32 SIMT GEMM with an explicit CTA tile and split-K factor.
+enum : int { kSimtTile128x128 = 0, kSimtTile128x64 = 1, kSimtTile64x128 = 2, kSimtTile64x64 = 3 };
+gbblas_status_t launch_gemm_simt_tiled(gbblas_handle_t h, const GemmArgs<float>& g, int tile, int split);
 gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<double>& g);
 
 // C <- beta*C over a strided batch of M x N matrices (beta == 0 writes zeros):
@@ -34,6 +37,14 @@ gbblas_status_t launch_scale_c(gbblas_handle_t h, int64_t m, int64_t n, double b
 // Split-BF16 FP32 GEMM on the tcgen05 tensor cores (pieces = 2 or 3 BF16
 // terms per operand).  Returns UNSUPPORTED when the shape is not handled.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces);
+// Same with an explicit N tile (64 or 128), split-K factor and raster order
+// (raster_m: consecutive CTAs walk down M).
+gbblas_status_t launch_gemm_split_bf16_cfg(gbblas_handle_t h, const GemmArgs<float>& g, int pieces, int bn,
+                                           int split, int raster_m);
+
+// Sums split-K partial tiles ws[batch][split][M][N] in slice order into C
+// with the alpha/beta epilogue (deterministic).
+gbblas_status_t launch_splitk_reduce(gbblas_handle_t h, const GemmArgs<float>& g, int split, const float* ws);
 
 // Method dispatch after argument checks (gemm.cu).
 gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g);

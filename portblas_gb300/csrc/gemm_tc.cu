@@ -65,12 +65,19 @@ enum : int { kErrTcProducer = 101, kErrTcMma = 102, kErrTcEpilogue = 103, kErrTc
 // k loop is cut into chunks of kTcChunk k-blocks, each accumulated in its
 // own TMEM buffer (two buffers, so the MMA warp runs one chunk ahead) and
 // added by the epilogue warps into a per-thread FP32 register row.
-template <int BN, int P, int STAGES>
+// Batches and split-K slices run on gridDim.z (z = batch * split + slice);
+// the operand terms of batch b are terms b*P .. b*P+P-1 of the tensor maps.
+// PARTIAL: split-K slice — the raw tile goes to ws[batch][split][M][N].
+template <int BN, int P, int STAGES, bool PARTIAL>
 __global__ void __launch_bounds__(kTcThreads, 1)
     gemm_split_bf16_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
-                           int M, int N, int nk, float alpha, float beta, float* __restrict__ C, int64_t ldc,
-                           int* __restrict__ err) {
+                           int M, int N, int nk_total, int split, int kb_per_split, float alpha, float beta,
+                           float* __restrict__ C, int64_t ldc, int64_t stride_c, float* __restrict__ ws,
+                           int raster_m, int* __restrict__ err) {
   using Cfg = TcCfg<BN, P, STAGES>;
+  const int bz = blockIdx.z / split, slice = blockIdx.z % split;
+  const int kb0 = slice * kb_per_split;
+  const int nk = max(0, min(nk_total - kb0, kb_per_split));
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* tiles = smem;
@@ -81,7 +88,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * kTcBM, n0 = blockIdx.x * BN;
+  // raster_m: consecutive CTAs walk down M (share a B tile) instead of along N
+  const int m0 = (raster_m ? blockIdx.x : blockIdx.y) * kTcBM;
+  const int n0 = (raster_m ? blockIdx.y : blockIdx.x) * BN;
   const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
 
   if (threadIdx.x == 0) {
@@ -119,10 +128,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
         uint8_t* st = tiles + s * Cfg::STAGE;
 #pragma unroll
-        for (int p = 0; p < P; ++p) tc::tma_load_3d(st + p * Cfg::A_TILE, &tma_a, &full[s], kb * kTcBK, m0, p);
+        for (int p = 0; p < P; ++p)
+          tc::tma_load_3d(st + p * Cfg::A_TILE, &tma_a, &full[s], (kb0 + kb) * kTcBK, m0, bz * P + p);
 #pragma unroll
         for (int p = 0; p < P; ++p)
-          tc::tma_load_3d(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, &full[s], kb * kTcBK, n0, p);
+          tc::tma_load_3d(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, &full[s], (kb0 + kb) * kTcBK, n0,
+                          bz * P + p);
         issued = kb + 1;
       }
       // drain: every copy this thread issued has landed before the CTA exits
@@ -202,14 +213,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (lane == 0) tc::mbar_arrive(&tempty[b]);
     }
     if (ok && gm < M) {
+      if (PARTIAL) {
+        float* W0 = ws + (int64_t(bz) * split + slice) * int64_t(M) * N;
 #pragma unroll
-      for (int i = 0; i < BN; ++i) {
-        const int gn = n0 + i;
-        if (gn < N) {
-          float* cp = C + int64_t(gm) + int64_t(gn) * ldc;
-          float v = alpha * sum[i];
-          if (beta != 0.f) v = fmaf(beta, *cp, v);
-          *cp = v;
+        for (int i = 0; i < BN; ++i) {
+          const int gn = n0 + i;
+          if (gn < N) W0[int64_t(gm) + int64_t(gn) * M] = sum[i];
+        }
+      } else {
+        float* Cb = C + int64_t(bz) * stride_c;
+#pragma unroll
+        for (int i = 0; i < BN; ++i) {
+          const int gn = n0 + i;
+          if (gn < N) {
+            float* cp = Cb + int64_t(gm) + int64_t(gn) * ldc;
+            float v = alpha * sum[i];
+            if (beta != 0.f) v = fmaf(beta, *cp, v);
+            *cp = v;
+          }
         }
       }
     }
@@ -228,9 +249,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // and the K-contiguous write are coalesced.
 template <int P>
 __global__ void __launch_bounds__(256) split_bf16_kernel(const float* __restrict__ X, int64_t sr, int64_t sk,
-                                                         int64_t R, int64_t K, int64_t Kp,
+                                                         int64_t R, int64_t K, int64_t Kp, int64_t xstride,
                                                          __nv_bfloat16* __restrict__ out) {
   __shared__ float t[32][33];  // t[k][r]
+  X += int64_t(blockIdx.z) * xstride;
+  out += int64_t(blockIdx.z) * P * R * Kp;
   const int64_t r0 = int64_t(blockIdx.y) * 32, k0 = int64_t(blockIdx.x) * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (sr == 1) {
@@ -300,71 +323,83 @@ static gbblas_status_t make_term_map(CUtensorMap* map, void* base, int64_t rows,
 
 template <int P>
 static gbblas_status_t launch_split(gbblas_handle_t h, const float* X, int64_t sr, int64_t sk, int64_t R, int64_t K,
-                                    int64_t Kp, __nv_bfloat16* out) {
-  dim3 grid(unsigned(Kp / 32), unsigned(cdiv(R, 32)));
-  if (grid.y > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: too many rows");
-  split_bf16_kernel<P><<<grid, dim3(32, 8), 0, h->stream>>>(X, sr, sk, R, K, Kp, out);
+                                    int64_t Kp, int64_t batch, int64_t xstride, __nv_bfloat16* out) {
+  dim3 grid(unsigned(Kp / 32), unsigned(cdiv(R, 32)), unsigned(batch));
+  if (grid.y > 65535 || grid.z > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
+  split_bf16_kernel<P><<<grid, dim3(32, 8), 0, h->stream>>>(X, sr, sk, R, K, Kp, xstride, out);
   return after_launch("split_bf16");
 }
 
-template <int BN, int P, int STAGES>
+template <int BN, int P, int STAGES, bool PARTIAL>
 static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb, int64_t M,
-                                 int64_t N, int64_t nk, float alpha, float beta, float* C, int64_t ldc) {
+                                 int64_t N, int64_t nk, int64_t batch, int split, float alpha, float beta, float* C,
+                                 int64_t ldc, int64_t stride_c, float* ws, int raster_m) {
   using Cfg = TcCfg<BN, P, STAGES>;
   static bool attr_set = false;
   if (!attr_set) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_bf16_kernel<BN, P, STAGES>,
+    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
     attr_set = true;
   }
-  dim3 grid(unsigned(cdiv(N, BN)), unsigned(cdiv(M, kTcBM)));
-  gemm_split_bf16_kernel<BN, P, STAGES><<<grid, kTcThreads, Cfg::SMEM, h->stream>>>(
-      ta, tb, int(M), int(N), int(nk), alpha, beta, C, ldc, h->dev_error);
+  const int kb_per = int(cdiv(nk, split));
+  const unsigned tn = unsigned(cdiv(N, BN)), tm = unsigned(cdiv(M, kTcBM));
+  dim3 grid(raster_m ? tm : tn, raster_m ? tn : tm, unsigned(batch * split));
+  if (grid.y > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
+  gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL><<<grid, kTcThreads, Cfg::SMEM, h->stream>>>(
+      ta, tb, int(M), int(N), int(nk), split, kb_per, alpha, beta, C, ldc, stride_c, ws, raster_m, h->dev_error);
   return after_launch("gemm_split_bf16");
 }
 
-template <int P>
-static gbblas_status_t split_gemm_one(gbblas_handle_t h, const GemmArgs<float>& g, const float* A, const float* B,
-                                      float* C) {
-  const int64_t M = g.m, N = g.n, K = g.k;
+template <int BN, int P>
+static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& g, int split, int raster_m) {
+  constexpr int STAGES = (P * (kTcBM + BN) * kTcBK * 2) <= 56 * 1024 ? 4 : ((P * (kTcBM + BN) * kTcBK * 2) <= 72 * 1024 ? 3 : 2);
+  const int64_t M = g.m, N = g.n, K = g.k, B = g.batch;
   const int64_t Kp = cdiv(K, kTcBK) * kTcBK;
-  const size_t a_bytes = size_t(P) * M * Kp * 2, b_bytes = size_t(P) * N * Kp * 2;
-  void* ws = nullptr;
-  GB_TRY(temp_acquire(h, ((a_bytes + 1023) & ~size_t(1023)) + b_bytes, &ws));
-  auto* at = static_cast<__nv_bfloat16*>(ws);
-  auto* bt = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(ws) + ((a_bytes + 1023) & ~size_t(1023)));
+  const int64_t nk = Kp / kTcBK;
+  if (split < 1) split = 1;
+  if (split > nk) split = int(nk);
+  split = int(cdiv(nk, cdiv(nk, split)));  // no empty slices
+  if (B * split > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: batch x split too large");
+  if (split > 1 && double(split) * double(M) * double(N) * double(B) > double(int64_t(1) << 28))
+    return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: split-K workspace too large");
+  const size_t a_bytes = (size_t(P) * M * Kp * 2 * B + 1023) & ~size_t(1023);
+  const size_t b_bytes = (size_t(P) * N * Kp * 2 * B + 1023) & ~size_t(1023);
+  const size_t w_bytes = split > 1 ? sizeof(float) * size_t(split) * M * N * B : 0;
+  void* wsp = nullptr;
+  GB_TRY(temp_acquire(h, a_bytes + b_bytes + w_bytes, &wsp));
+  auto* at = static_cast<__nv_bfloat16*>(wsp);
+  auto* bt = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(wsp) + a_bytes);
+  float* ws = split > 1 ? reinterpret_cast<float*>(static_cast<uint8_t*>(wsp) + a_bytes + b_bytes) : nullptr;
   // A(m, k): (ta ? A[k + m*lda] : A[m + k*lda]);  B as rows n: (tb ? B[n + k*ldb] : B[k + n*ldb])
-  GB_TRY(launch_split<P>(h, A, g.ta ? g.lda : 1, g.ta ? 1 : g.lda, M, K, Kp, at));
-  GB_TRY(launch_split<P>(h, B, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, K, Kp, bt));
-  constexpr int BN = 128;
-  constexpr int STAGES = P == 3 ? 2 : (P == 2 ? 3 : 6);
+  GB_TRY(launch_split<P>(h, g.a, g.ta ? g.lda : 1, g.ta ? 1 : g.lda, M, K, Kp, B, g.stride_a, at));
+  GB_TRY(launch_split<P>(h, g.b, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, K, Kp, B, g.stride_b, bt));
   CUtensorMap ma, mb;
-  GB_TRY(make_term_map(&ma, at, M, Kp, P, kTcBM));
-  GB_TRY(make_term_map(&mb, bt, N, Kp, P, BN));
-  return launch_tc<BN, P, STAGES>(h, ma, mb, M, N, Kp / kTcBK, g.alpha, g.beta, C, g.ldc);
+  GB_TRY(make_term_map(&ma, at, M, Kp, P * B, kTcBM));
+  GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, BN));
+  if (split == 1)
+    return launch_tc<BN, P, STAGES, false>(h, ma, mb, M, N, nk, B, 1, g.alpha, g.beta, g.c, g.ldc, g.stride_c,
+                                           nullptr, raster_m);
+  GB_TRY((launch_tc<BN, P, STAGES, true>(h, ma, mb, M, N, nk, B, split, g.alpha, g.beta, g.c, g.ldc, g.stride_c,
+                                         ws, raster_m)));
+  return launch_splitk_reduce(h, g, split, ws);
 }
 
-gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
+gbblas_status_t launch_gemm_split_bf16_cfg(gbblas_handle_t h, const GemmArgs<float>& g, int pieces, int bn,
+                                           int split, int raster_m) {
   if (pieces != 2 && pieces != 3) return fail(GBBLAS_STATUS_INVALID_ARG, "split-BF16 GEMM: pieces must be 2 or 3");
   if (g.m > INT32_MAX / 2 || g.n > INT32_MAX / 2 || g.k > INT32_MAX / 2)
     return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: dimension too large");
   if (g.k == 0) return launch_scale_c(h, g.m, g.n, g.beta, g.c, g.ldc, g.stride_c, g.batch);
-  for (int64_t b = 0; b < g.batch; ++b) {
-    const float* A = g.a + b * g.stride_a;
-    const float* B = g.b + b * g.stride_b;
-    float* C = g.c + b * g.stride_c;
-    GB_TRY(pieces == 2 ? split_gemm_one<2>(h, g, A, B, C) : split_gemm_one<3>(h, g, A, B, C));
-  }
-  return GBBLAS_STATUS_SUCCESS;
+  if (bn == 64)
+    return pieces == 2 ? split_gemm_run<64, 2>(h, g, split, raster_m) : split_gemm_run<64, 3>(h, g, split, raster_m);
+  if (bn == 128)
+    return pieces == 2 ? split_gemm_run<128, 2>(h, g, split, raster_m)
+                       : split_gemm_run<128, 3>(h, g, split, raster_m);
+  return fail(GBBLAS_STATUS_INVALID_ARG, "split-BF16 GEMM: N tile must be 64 or 128");
 }
 
-// AUTO: the FP32-accurate 3-term split on the tensor cores for single
-// problems large enough to amortise the split pass; SIMT otherwise.
-int select_sgemm_method(gbblas_handle_t, const GemmArgs<float>& g) {
-  const double work = double(g.m) * double(g.n) * double(g.k);
-  if (g.batch == 1 && g.m >= 256 && g.n >= 256 && g.k >= 128 && work >= double(1 << 27))
-    return GBBLAS_SGEMM_SPLIT_BF16X6;
-  return GBBLAS_SGEMM_FP32_SIMT;
+gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
+  return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 0);
 }
 
 }  // namespace gb
