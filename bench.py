@@ -314,6 +314,117 @@ def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
     return res
 
 
+def bench_batched(torch, blas, sb, dev, reps=10):
+    """BASELINE config 4: a grouped batch of 2048 problems with M, N, K each
+    log-uniform in [16, 512] (seeded), random transposes, FP32 and BF16 inputs
+    (FP32 accumulate), as one persistent launch replayed from a CUDA graph;
+    and a strided batch of 4096 x 64^3 FP32."""
+    g = np.random.default_rng(4)
+    count = 2048
+    dims = np.round(np.exp(g.uniform(np.log(16), np.log(512), (count, 3)))).astype(int)
+    trans = g.integers(0, 2, (count, 2))
+    flops = float(2 * np.prod(dims, axis=1).sum())
+    out = {"grouped": {"problems": count, "flop_per_call": flops}}
+    for dt in ("float32", "bfloat16"):
+        tdt = torch.float32 if dt == "float32" else torch.bfloat16
+        probs, bytes_in = [], 0
+        for (m, n, k), (ta, tb) in zip(dims, trans):
+            a = torch.rand(int(m * k), device=dev, dtype=torch.float32).to(tdt)
+            b = torch.rand(int(k * n), device=dev, dtype=torch.float32).to(tdt)
+            c = torch.empty(int(m * n), device=dev)
+            bytes_in += a.numel() * a.element_size() + b.numel() * b.element_size() + c.numel() * 4
+            probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=int(m), n=int(n), k=int(k),
+                              alpha=1.0, a=a, lda=int(k if ta else m), b=b, ldb=int(n if tb else k), beta=0.0, c=c,
+                              ldc=int(m)))
+        plan = blas.GroupedPlan(sb, probs, dtype=dt)
+        for _ in range(3):
+            plan.run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            plan.run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out["grouped"][dt] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
+                              "gbs": bytes_in / (ms * 1e-3) / 1e9, "bytes_per_call": bytes_in}
+        plan.close()
+        del probs
+    # strided batch 4096 x 64^3 FP32 (A, B, C 64 MiB each)
+    nb, n = 4096, 64
+    A = torch.rand(nb * n * n, device=dev)
+    B = torch.rand(nb * n * n, device=dev)
+    Cc = torch.empty(nb * n * n, device=dev)
+    f = 2.0 * nb * n ** 3
+    byt = 3 * nb * n * n * 4
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    for _ in range(3):
+        blas._gemm_strided_batched(sb, "n", "n", n, n, n, 1.0, A, n, n * n, B, n, n * n, 0.0, Cc, n, n * n, nb)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        blas._gemm_strided_batched(sb, "n", "n", n, n, n, 1.0, A, n, n * n, B, n, n * n, 0.0, Cc, n, n * n, nb)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ref = (A[: n * n].view(n, n).T.double() @ B[: n * n].view(n, n).T.double())
+    err = float((Cc[: n * n].view(n, n).T.double() - ref).abs().max().item())
+    out["strided_4096x64"] = {"ms": ms, "tflops": f / (ms * 1e-3) / 1e12, "gbs": byt / (ms * 1e-3) / 1e9,
+                              "max_abs_err_first": err}
+    return out
+
+
+def bench_selector(torch, blas, sb, dev, shapes=48):
+    """BASELINE config 5 spot check: regret of the learned selector and of the
+    size heuristic against exhaustive timing on fresh seeded shapes (the full
+    1000-shape held-out evaluation is in tuning/sgemm_selector_report.json)."""
+    import ctypes as C
+    from portblas_gb300 import _lib
+    from portblas_gb300.tuning import sweep
+    L = _lib.load()
+    rep_path = os.path.join(ROOT, "portblas_gb300", "tuning", "sgemm_selector_report.json")
+    report = json.load(open(rep_path)) if os.path.exists(rep_path) else None
+    ss = sweep.sample_shapes(shapes, seed=987654)
+    A = torch.rand(sweep.ELEM_CAP + 4096, device=dev)
+    B = torch.rand(sweep.ELEM_CAP + 4096, device=dev)
+    Cm = torch.zeros(sweep.ELEM_CAP + 65536, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r_mlp, r_heur = [], []
+    for s in ss:
+        m, n, k, bt = s["m"], s["n"], s["k"], s["batch"]
+        sa = (m * s["lda"]) if s["ta"] else (k * s["lda"])
+        sbs = (k * s["ldb"]) if s["tb"] else (n * s["ldb"])
+        sc = n * s["ldc"]
+        bt = max(1, min(bt, (sweep.ELEM_CAP + 4096) // max(sa, sbs, sc)))
+        ta, tb = (b"t" if s["ta"] else b"n"), (b"t" if s["tb"] else b"n")
+        t = np.full(40, np.inf)
+        for c in range(40):
+            run = lambda: L.gbblas_sgemm_strided_batched_config(sb.handle, c, ta, tb, m, n, k, 1.0, A.data_ptr(),
+                                                                s["lda"], sa, B.data_ptr(), s["ldb"], sbs, 0.0,
+                                                                Cm.data_ptr(), s["ldc"], sc, bt)
+            if run() != 0:
+                continue
+            e0.record()
+            for _ in range(3):
+                run()
+            e1.record()
+            e1.synchronize()
+            t[c] = e0.elapsed_time(e1) / 3
+        pick = C.c_int()
+        L.gbblas_sgemm_selector_pick(m, n, k, ta, tb, s["lda"], s["ldb"], s["ldc"], bt, C.byref(pick))
+        h = L.gbblas_sgemm_heuristic_config(m, n, k, bt)
+        r_mlp.append(t[pick.value] / t.min() - 1)
+        r_heur.append(t[h] / t.min() - 1)
+    out = {"live_shapes": shapes, "live_regret_mean": {"mlp": float(np.mean(r_mlp)),
+                                                       "heuristic": float(np.mean(r_heur))}}
+    if report:
+        out["heldout"] = {k: report[k] for k in ("heldout_shapes", "regret_mean", "total_time_over_exhaustive",
+                                                 "train_seconds") if k in report}
+    return out
+
+
 # ----------------------------------------------------------- CPU side --
 def cpu_reference_step(cb, oracle_mod, data, outs):
     """The memory-bound step on the host cores: OpenBLAS CBLAS + OpenMP C
@@ -369,7 +480,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-sgemm", action="store_true", help="skip the SGEMM/DGEMM set")
-    ap.add_argument("--profile", choices=["memory", "sgemm"], default=None,
+    ap.add_argument("--profile", choices=["memory", "sgemm", "batched"], default=None,
                     help="short run of one workload only (no e2e, CPU baseline or JSON line), for ncu captures")
     ap.add_argument("--sgemm-n", type=int, default=8192)
     args = ap.parse_args()
@@ -414,6 +525,9 @@ def main():
         r = bench_memory_set(torch, blas, sb, args.steps, args.warmup, dev, per_op_reps=0)
         print(json.dumps({"profile": "memory", "ms_per_step": r["ms"]}))
         return
+    if args.profile == "batched":
+        print(json.dumps({"profile": "batched", "res": bench_batched(torch, blas, sb, dev, reps=2)}))
+        return
     if args.profile == "sgemm":
         r = bench_sgemm(torch, blas, sb, dev, reps=1, n=args.sgemm_n, with_dgemm=False)
         print(json.dumps({"profile": "sgemm", "n": args.sgemm_n, "res": r}))
@@ -433,9 +547,11 @@ def main():
     ab = algorithmic_bytes()
     dom = max(mem["per_op"], key=lambda n: mem["per_op"][n])
     achieved = ab[dom] / (mem["per_op"][dom] * 1e-3) / 1e9
-    sg = None
+    sg = bat = sel = None
     if not args.no_sgemm:
         sg = bench_sgemm(torch, blas, sb, dev)
+        bat = bench_batched(torch, blas, sb, dev)
+        sel = bench_selector(torch, blas, sb, dev)
     if rank != 0:
         return
     cpu = bench_cpu(2, 1, budget_s=15.0)
@@ -455,6 +571,8 @@ def main():
                          "sample": f"{cpu['steps']} full memory-bound steps on the host (OpenBLAS CBLAS + "
                                    "OpenMP C Reduction restatement), median"},
         "sgemm": sg,
+        "batched": bat,
+        "selector": sel,
     }
     print(json.dumps(line), flush=True)
 

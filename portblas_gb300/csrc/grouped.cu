@@ -20,10 +20,13 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <new>
 #include <vector>
 
 #include "gemm_internal.cuh"
+#include "grouped_tc.cuh"
 
 namespace gb {
 
@@ -151,6 +154,7 @@ __global__ void __launch_bounds__(kGThreads) grouped_gemm_kernel(const GroupedPr
 // instantiated CUDA graph of the persistent launch.
 struct gbblas_grouped_plan_s {
   int dtype = 0;
+  int method = 1;  // 1: tcgen05 tiles (128 x 64), 0: SIMT tiles (64 x 64)
   int count = 0;
   int64_t total_tiles = 0;
   int grid = 0;
@@ -158,16 +162,45 @@ struct gbblas_grouped_plan_s {
   unsigned long long* counters = nullptr;
   cudaGraphExec_t exec = nullptr;
   int device = 0;
+  int* err = nullptr;  // device error word of the creating handle
 };
 
 using namespace gb;
 
-static gbblas_status_t launch_grouped(cudaStream_t s, gbblas_grouped_plan_s* p) {
+static gbblas_status_t launch_grouped(cudaStream_t s, gbblas_grouped_plan_s* p, int* err) {
+  if (p->method == 1) {
+    if (p->dtype == GBBLAS_DTYPE_BF16) {
+      static bool attr = false;
+      if (!attr) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<__nv_bfloat16, 1, GroupedProblem>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<1>::SMEM));
+        attr = true;
+      }
+      grouped_tc_kernel<__nv_bfloat16, 1, GroupedProblem><<<p->grid, kGtThreads, GtCfg<1>::SMEM, s>>>(
+          p->table, p->count, p->total_tiles, p->counters, err);
+    } else {
+      static bool attr = false;
+      if (!attr) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<float, 3, GroupedProblem>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<3>::SMEM));
+        attr = true;
+      }
+      grouped_tc_kernel<float, 3, GroupedProblem><<<p->grid, kGtThreads, GtCfg<3>::SMEM, s>>>(
+          p->table, p->count, p->total_tiles, p->counters, err);
+    }
+    return after_launch("grouped_tc");
+  }
   if (p->dtype == GBBLAS_DTYPE_BF16)
     grouped_gemm_kernel<__nv_bfloat16><<<p->grid, kGThreads, 0, s>>>(p->table, p->count, p->total_tiles, p->counters);
   else
     grouped_gemm_kernel<float><<<p->grid, kGThreads, 0, s>>>(p->table, p->count, p->total_tiles, p->counters);
   return after_launch("grouped_gemm");
+}
+
+// Tile kernel of a grouped launch: tcgen05 unless GBBLAS_GROUPED_METHOD=simt.
+static int grouped_method() {
+  const char* e = std::getenv("GBBLAS_GROUPED_METHOD");
+  return (e && std::strcmp(e, "simt") == 0) ? 0 : 1;
 }
 
 extern "C" gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t plan) {
@@ -183,7 +216,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
                                    const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
                                    const void* const* a, const int64_t* lda, const void* const* b,
                                    const int64_t* ldb, const float* beta, float* const* c, const int64_t* ldc,
-                                   std::vector<GroupedProblem>& tab, int64_t& tiles) {
+                                   int tile_m, int tile_n, std::vector<GroupedProblem>& tab, int64_t& tiles) {
   if (dtype != GBBLAS_DTYPE_F32 && dtype != GBBLAS_DTYPE_BF16)
     return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: element type must be F32 or BF16");
   if (count < 0 || count > (1 << 24)) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: bad problem count");
@@ -209,7 +242,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
     p.k = alpha[i] == 0.f ? 0 : int(k[i]);
     p.ta = ca != 'n';
     p.tb = cb != 'n';
-    p.tiles_n = int(cdiv(n[i], kGT));
+    p.tiles_n = int(cdiv(n[i], tile_n));
     p.tile_start = tiles;
     p.alpha = alpha[i];
     p.beta = beta[i];
@@ -219,14 +252,16 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
     p.lda = lda[i];
     p.ldb = ldb[i];
     p.ldc = ldc[i];
-    tiles += cdiv(m[i], kGT) * p.tiles_n;
+    tiles += cdiv(m[i], tile_m) * p.tiles_n;
     tab.push_back(p);
   }
   return GBBLAS_STATUS_SUCCESS;
 }
 
-static int grouped_grid(gbblas_handle_t h, int64_t tiles) {
-  const int64_t cap = int64_t(h->sm_count) * 8;  // 8 resident 256-thread CTAs per SM
+static int grouped_grid(gbblas_handle_t h, int64_t tiles, int method, int dtype) {
+  // resident CTAs per SM: SIMT 8 x 256 threads; tcgen05 by shared memory
+  const int per_sm = method == 0 ? 8 : (dtype == GBBLAS_DTYPE_BF16 ? 4 : 1);
+  const int64_t cap = int64_t(h->sm_count) * per_sm;
   return int(std::max<int64_t>(1, std::min<int64_t>(tiles, cap)));
 }
 
@@ -244,14 +279,18 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
   *out = nullptr;
   std::vector<GroupedProblem> tab;
   int64_t tiles = 0;
-  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tab, tiles));
+  const int method = grouped_method();
+  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                     method ? kGtBM : kGT, method ? kGtBN : kGT, tab, tiles));
   auto* plan = new (std::nothrow) gbblas_grouped_plan_s();
   if (!plan) return fail(GBBLAS_STATUS_ALLOC_FAILED, "grouped: out of host memory");
   plan->dtype = dtype;
+  plan->method = method;
+  plan->err = h->dev_error;
   plan->count = int(tab.size());
   plan->total_tiles = tiles;
   plan->device = h->device;
-  plan->grid = grouped_grid(h, tiles);
+  plan->grid = grouped_grid(h, tiles, method, dtype);
   cudaError_t e = cudaMalloc(&plan->table, sizeof(GroupedProblem) * std::max<size_t>(1, tab.size()));
   if (e == cudaSuccess) e = cudaMalloc(&plan->counters, 2 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(plan->counters, 0, 2 * sizeof(unsigned long long));
@@ -278,7 +317,7 @@ gbblas_status_t gbblas_grouped_plan_run(gbblas_handle_t h, gbblas_grouped_plan_t
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      gbblas_status_t s = launch_grouped(cs, plan);
+      gbblas_status_t s = launch_grouped(cs, plan, plan->err);
       e = cudaStreamEndCapture(cs, &graph);
       if (s != GBBLAS_STATUS_SUCCESS && e == cudaSuccess) e = cudaErrorLaunchFailure;
     }
@@ -303,7 +342,9 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
   if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "grouped: null handle");
   std::vector<GroupedProblem> tab;
   int64_t tiles = 0;
-  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tab, tiles));
+  const int method = grouped_method();
+  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                     method ? kGtBM : kGT, method ? kGtBN : kGT, tab, tiles));
   if (tiles == 0) return GBBLAS_STATUS_SUCCESS;
   // one-shot: table and counters live in the handle's stream-ordered temp memory
   const size_t tbytes = (sizeof(GroupedProblem) * tab.size() + 255) & ~size_t(255);
@@ -311,15 +352,16 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
   GB_TRY(temp_acquire(h, tbytes + 256, &ws));
   gbblas_grouped_plan_s tmp;
   tmp.dtype = dtype;
+  tmp.method = method;
   tmp.count = int(tab.size());
   tmp.total_tiles = tiles;
-  tmp.grid = grouped_grid(h, tiles);
+  tmp.grid = grouped_grid(h, tiles, method, dtype);
   tmp.table = static_cast<GroupedProblem*>(ws);
   tmp.counters = reinterpret_cast<unsigned long long*>(static_cast<uint8_t*>(ws) + tbytes);
   GB_CUDA_TRY(cudaMemcpyAsync(tmp.table, tab.data(), sizeof(GroupedProblem) * tab.size(), cudaMemcpyHostToDevice,
                               h->stream));
   GB_CUDA_TRY(cudaMemsetAsync(tmp.counters, 0, 2 * sizeof(unsigned long long), h->stream));
-  gbblas_status_t s = launch_grouped(h->stream, &tmp);
+  gbblas_status_t s = launch_grouped(h->stream, &tmp, h->dev_error);
   tmp.table = nullptr;  // not owned
   tmp.counters = nullptr;
   return s;

@@ -41,16 +41,50 @@ def _check(probs, host):
         np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * max(1, k))
 
 
+METHODS = ["tcgen05", "simt"]
+
+
+@pytest.fixture
+def method(request, monkeypatch):
+    monkeypatch.setenv("GBBLAS_GROUPED_METHOD", request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("method", METHODS, indirect=True)
 @pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
-def test_grouped_one_shot(sb, torch_cuda, dtype):
+def test_grouped_one_shot(sb, torch_cuda, dtype, method):
     from portblas_gb300 import blas
     probs, host = _problems(torch_cuda, rng(31), 64, 1, 300, dtype)
     blas._gemm_grouped(sb, probs, dtype=dtype)
     _check(probs, host)
+    sb.check_device_error()
 
 
+@pytest.mark.parametrize("method", METHODS, indirect=True)
+def test_grouped_long_k_accuracy(sb, torch_cuda, method):
+    """K well past the accumulator promotion interval: FP32-level accuracy."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(43)
+    probs, host = [], []
+    for (m, n, k) in [(130, 70, 3000), (64, 200, 1100), (1, 1, 5000)]:
+        a = (g.choice([-1.0, 1.0], m * k) * np.exp2(g.uniform(-8, 8, m * k))).astype(np.float32)
+        b = (g.choice([-1.0, 1.0], k * n) * np.exp2(g.uniform(-8, 8, k * n))).astype(np.float32)
+        c = np.zeros(m * n, np.float32)
+        probs.append(dict(transa="n", transb="n", m=m, n=n, k=k, alpha=1.0, a=torch.from_numpy(a).cuda(), lda=m,
+                          b=torch.from_numpy(b).cuda(), ldb=k, beta=0.0, c=torch.from_numpy(c).cuda(), ldc=m))
+        host.append((m, n, k, a, b))
+    blas._gemm_grouped(sb, probs, dtype="float32")
+    for p, (m, n, k, a, b) in zip(probs, host):
+        ref = oracle.gemm(False, False, m, n, k, 1.0, a, m, b, k, 0.0, None, m)
+        scale = oracle.gemm_absscale(False, False, m, n, k, 1.0, a, m, b, k, 0.0, None, m)
+        got = p["c"].cpu().numpy().reshape(n, m).T
+        assert (np.abs(got - ref) / scale).max() <= 2.0 * (k + 4) * 2.0 ** -24
+
+
+@pytest.mark.parametrize("method", METHODS, indirect=True)
 @pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
-def test_grouped_plan_graph_replay(sb, torch_cuda, dtype):
+def test_grouped_plan_graph_replay(sb, torch_cuda, dtype, method):
     """The captured graph replays correctly, twice (scheduler counters reset)."""
     torch = torch_cuda
     from portblas_gb300 import blas
