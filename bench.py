@@ -168,12 +168,18 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev, per_op_reps=None):
         run_step(blas, sb, inp, outs)
     torch.cuda.synchronize()
     # per-op device times (events around each op, separate pass)
+    # per-op device times: events around each op, steps enqueued back to back
+    # (no host sync in between, so the queue stays ahead of the GPU and no
+    # host launch gap lands inside an op's window); median over the steps
     per_op = {n: [] for n in names}
     reps = max(3, min(steps, 10)) if per_op_reps is None else per_op_reps
+    evs = []
     for _ in range(reps):
         ev = {n: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for n in names}
         run_step(blas, sb, inp, outs, ev)
-        torch.cuda.synchronize()
+        evs.append(ev)
+    torch.cuda.synchronize()
+    for ev in evs[1:] if len(evs) > 1 else evs:
         for n in names:
             per_op[n].append(ev[n][0].elapsed_time(ev[n][1]))
     # the timed region: K whole steps between two events

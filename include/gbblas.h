@@ -191,7 +191,8 @@ gbblas_status_t gbblas_dgemm(gbblas_handle_t h, char transa, char transb, int64_
 /* blas::_gemm_batched (include/interface/blas3_interface.h:97-109;
  *   src/interface/gemm_interface.hpp:200-226).  Strided batch with the
  *   default strides (ta? m*lda : k*lda), (tb? ldb*k : n*ldb), ldc*n; the
- *   interleaved batch type keeps batch as the fastest axis. */
+ *   interleaved batch type keeps batch as the fastest axis: element (r, c)
+ *   of matrix b is at ptr[(r + c*ld)*batch + b]. */
 gbblas_status_t gbblas_sgemm_batched(gbblas_handle_t h, char transa, char transb, int64_t m, int64_t n,
                                      int64_t k, float alpha, const float* a, int64_t lda, const float* b,
                                      int64_t ldb, float beta, float* c, int64_t ldc, int64_t batch_size,

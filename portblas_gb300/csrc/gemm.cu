@@ -66,9 +66,22 @@ template <typename T>
 gbblas_status_t batched_front(gbblas_handle_t h, char ta, char tb, int64_t m, int64_t n, int64_t k, T alpha,
                                      const T* a, int64_t lda, const T* b, int64_t ldb, T beta, T* c, int64_t ldc,
                                      int64_t batch, int batch_type) {
-  if (batch_type == GBBLAS_BATCH_INTERLEAVED)
-    return fail(GBBLAS_STATUS_UNSUPPORTED, "gemm_batched: interleaved batch type is not implemented");
-  if (batch_type != GBBLAS_BATCH_STRIDED) return fail(GBBLAS_STATUS_INVALID_ARG, "gemm_batched: unknown batch type");
+  if (batch_type == GBBLAS_BATCH_INTERLEAVED && batch > 1) {
+    if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "gemm: null handle");
+    if (m < 0 || n < 0 || k < 0) return fail(GBBLAS_STATUS_INVALID_ARG, "gemm: negative dimension");
+    if (m == 0 || n == 0) return GBBLAS_STATUS_SUCCESS;
+    bool tra = false, trb = false;
+    if (alpha != T(0)) {
+      if (!parse_trans(ta, &tra)) return fail(GBBLAS_STATUS_INVALID_ARG, "invalid _TransA");
+      if (!parse_trans(tb, &trb)) return fail(GBBLAS_STATUS_INVALID_ARG, "invalid _TransB");
+      if (k > 0 && (!a || !b)) return fail(GBBLAS_STATUS_INVALID_ARG, "gemm: null A or B");
+    }
+    if (!c) return fail(GBBLAS_STATUS_INVALID_ARG, "gemm: null C");
+    GemmArgs<T> g{tra, trb, m, n, k, alpha, beta, a, lda, 0, b, ldb, 0, c, ldc, 0, batch};
+    return launch_gemm_interleaved(h, g);
+  }
+  if (batch_type != GBBLAS_BATCH_STRIDED && batch_type != GBBLAS_BATCH_INTERLEAVED)
+    return fail(GBBLAS_STATUS_INVALID_ARG, "gemm_batched: unknown batch type");
   const bool tra = std::tolower(static_cast<unsigned char>(ta)) != 'n';
   const bool trb = std::tolower(static_cast<unsigned char>(tb)) != 'n';
   const int64_t sa = tra ? m * lda : k * lda;

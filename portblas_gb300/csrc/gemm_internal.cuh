@@ -22,6 +22,10 @@ struct GemmArgs {
 
 // Plain FP32 / FP64 SIMT GEMM (CUDA cores), any transposes, strided batch.
 gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<float>& g);
+// Interleaved batch (batch fastest): element (r, c) of matrix b at
+// ptr[(r + c*ld)*batch + b].
+gbblas_status_t launch_gemm_interleaved(gbblas_handle_t h, const GemmArgs<float>& g);
+gbblas_status_t launch_gemm_interleaved(gbblas_handle_t h, const GemmArgs<double>& g);
 // FP32 SIMT GEMM with an explicit CTA tile and split-K factor.
 enum : int { kSimtTile128x128 = 0, kSimtTile128x64 = 1, kSimtTile64x128 = 2, kSimtTile64x64 = 3 };
 gbblas_status_t launch_gemm_simt_tiled(gbblas_handle_t h, const GemmArgs<float>& g, int tile, int split);

@@ -231,3 +231,34 @@ def test_split_bf16x6_is_fp32_accurate(sb, torch_cuda, ta):
     assert x6_mean <= 2.0 * simt_mean + 1e-9, errs
     assert x6_max <= 4.0 * simt_max + 1e-8, errs
     assert errs["split_bf16x3"][1] <= 6e-5, errs  # the dropped 2^-16 terms bound the 2-term split
+
+
+def _to_interleaved(mats, ld_rows, ld_cols):
+    """Batch-fastest layout of a list of column-major ld_rows x ld_cols
+    matrices: element (r, c) of matrix b at [(r + c*ld_rows)*batch + b]
+    (test/unittest/blas3/blas3_gemm_common.hpp:53-69)."""
+    stack = np.stack([m[: ld_rows * ld_cols] for m in mats])  # [batch][ld_rows*ld_cols]
+    return np.ascontiguousarray(stack.T).ravel()
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("m,n,k,batch", [(4, 4, 4, 1000), (5, 3, 7, 129), (16, 20, 9, 64)])
+@pytest.mark.parametrize("alpha,beta", [(1.5, 0.5), (1.0, 0.0), (0.0, 2.0)])
+def test_gemm_batched_interleaved(sb, torch_cuda, ta, tb, m, n, k, batch, alpha, beta):
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(m + n + k + batch)
+    lda, ldb, ldc = (k if ta else m), (n if tb else k), m
+    acols, bcols = (m if ta else k), (k if tb else n)
+    As = [g.uniform(-2, 5, lda * acols).astype(np.float32) for _ in range(batch)]
+    Bs = [g.uniform(-2, 5, ldb * bcols).astype(np.float32) for _ in range(batch)]
+    Cs = [g.uniform(-2, 5, ldc * n).astype(np.float32) for _ in range(batch)]
+    cd = to_dev(_to_interleaved(Cs, ldc, n), torch)
+    blas._gemm_batched(sb, "t" if ta else "n", "t" if tb else "n", m, n, k, alpha,
+                       to_dev(_to_interleaved(As, lda, acols), torch), lda,
+                       to_dev(_to_interleaved(Bs, ldb, bcols), torch), ldb, beta, cd, ldc, batch,
+                       blas.gemm_batch_type_t.interleaved)
+    out = to_host(cd).reshape(ldc * n, batch).T  # back to [batch][ldc*n]
+    for i in range(0, batch, max(1, batch // 7)):
+        ref = oracle.gemm(ta, tb, m, n, k, alpha, As[i], lda, Bs[i], ldb, beta, Cs[i], ldc)
+        assert_almost_equal(out[i].reshape(n, ldc).T[:m], ref)
