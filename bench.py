@@ -56,6 +56,17 @@ def algorithmic_bytes() -> dict:
     }
 
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# each kernel of the step, from one ncu --set full capture of
+# `bench.py --profile memory --steps 1 --warmup 1` on a GB300, in bytes.
+NCU_TRAFFIC = {
+    "gemv_n": 0.268490e9 + 3.769088e6, "reduction_outer": 1.073866e9 + 3.405824e6,
+    "gemv_t": 0.268530e9 + 4.135424e6, "reduction_inner": 1.073791e9 + 3.998464e6,
+    "asum": 268.461312e6 + 3.583232e6, "nrm2": 268.470272e6 + 3.610624e6, "dot": 536.927232e6 + 3.253248e6,
+    "iamax": 268.471296e6 + 3.544320e6, "iamin": 268.47e6 + 3.6e6,
+}
+
+
 def peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -569,7 +580,9 @@ def main():
         "per_op": {n: {"ms": t, "gbs": ab[n] / (t * 1e-3) / 1e9, "frac": ab[n] / (t * 1e-3) / 1e9 / pk["hbm_gbs"]}
                    for n, t in mem["per_op"].items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "peak_src": pk["src"], "traffic": None},
+                     "frac": achieved / pk["hbm_gbs"], "peak_src": pk["src"],
+                     "traffic": NCU_TRAFFIC.get(dom), "traffic_unit": "bytes per launch (ncu)",
+                     "algorithmic_bytes": ab[dom]},
         "e2e": {"value": world * total_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
                 "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]},
         "gpu_launches": mem["launches"], "clocks": mem["clocks"], "checks": mem["checks"],

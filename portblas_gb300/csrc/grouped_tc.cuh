@@ -54,28 +54,44 @@ __device__ __forceinline__ float ld_f32<float>(const float* p) { return __ldg(p)
 template <>
 __device__ __forceinline__ float ld_f32<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 
-// Gathers 8 consecutive k of row `r` (global row gr) of an operand whose
-// element (row, k) is at src[row*srow + k*sk], splits them into P BF16
-// terms and stores one 16-byte chunk per term.
-template <typename T, int P>
-__device__ __forceinline__ void gather_chunk(const T* src, int64_t srow, int64_t sk, int64_t gr, int64_t rows,
-                                             int64_t k0, int64_t K, uint8_t* tile0, int tile_bytes, int r, int c) {
-  float v[8];
-  const int64_t kb = k0 + c * 8;
+// Gathers NCH chunks of 8 consecutive k of one row (global row gr) of an
+// operand whose element (row, k) is at src[row*srow + k*sk]: load() issues
+// every global load of the k-block first (so they are all in flight
+// together), store() splits the values into P BF16 terms and writes one
+// 16-byte swizzled chunk per term.
+template <typename T, int NCH>
+struct RowGather {
+  float v[NCH][8];
+  __device__ __forceinline__ void load(const T* src, int64_t srow, int64_t sk, int64_t gr, int64_t rows, int64_t k0,
+                                       int64_t K, int c0) {
+    const bool row_ok = gr < rows;
+    const T* p = src + (row_ok ? gr : 0) * srow;
 #pragma unroll
-  for (int e = 0; e < 8; ++e) v[e] = (gr < rows && kb + e < K) ? ld_f32<T>(src + gr * srow + (kb + e) * sk) : 0.f;
-  const uint32_t off = sw128_offset(r, c);
+    for (int c = 0; c < NCH; ++c)
 #pragma unroll
-  for (int p = 0; p < P; ++p) {
-    __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      h[e] = __float2bfloat16_rn(v[e]);
-      v[e] -= __bfloat162float(h[e]);  // exact residual for the next term
-    }
-    *reinterpret_cast<uint4*>(tile0 + p * tile_bytes + off) = *reinterpret_cast<const uint4*>(h);
+      for (int e = 0; e < 8; ++e) {
+        const int64_t kk = k0 + (c0 + c) * 8 + e;
+        v[c][e] = (row_ok && kk < K) ? ld_f32<T>(p + kk * sk) : 0.f;
+      }
   }
-}
+  template <int P>
+  __device__ __forceinline__ void store(uint8_t* tile0, int tile_bytes, int r, int c0) {
+#pragma unroll
+    for (int c = 0; c < NCH; ++c) {
+      const uint32_t off = sw128_offset(r, c0 + c);
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          h[e] = __float2bfloat16_rn(v[c][e]);
+          v[c][e] -= __bfloat162float(h[e]);  // exact residual for the next term
+        }
+        *reinterpret_cast<uint4*>(tile0 + p * tile_bytes + off) = *reinterpret_cast<const uint4*>(h);
+      }
+    }
+  }
+};
 
 enum : int { kErrGtFull = 401, kErrGtEmpty = 402, kErrGtAcc = 403 };
 
@@ -145,26 +161,26 @@ __global__ void __launch_bounds__(kGtThreads, 1)
     float sum[kGtBN];
 #pragma unroll
     for (int i = 0; i < kGtBN; ++i) sum[i] = 0.f;
+    RowGather<T, 8> ga;
+    RowGather<T, 4> gbt;
     bool ok = true;
     for (int kb = 0; kb < nk && ok; ++kb, ++it) {
       const int s = it % Cfg::STAGES;
       const uint32_t ph = (it / Cfg::STAGES) & 1;
+      uint8_t* st = smem + s * Cfg::STAGE;
+      const int64_t k0 = int64_t(kb) * kGtBK;
+      // A: thread t owns row t (8 chunks); B: 64 rows x 8 chunks over 128 threads.
+      // The loads go out before the wait for the stage, overlapping the MMAs
+      // still reading it.
+      ga.load(A, a_srow, a_sk, m0 + t, pr.m, k0, pr.k, 0);
+      gbt.load(B, b_srow, b_sk, n0 + (t & 63), pr.n, k0, pr.k, (t >> 6) * 4);
       if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
         if (t == 0) atomicExch(err, kErrGtEmpty);
         ok = false;
         break;
       }
-      uint8_t* st = smem + s * Cfg::STAGE;
-      const int64_t k0 = int64_t(kb) * kGtBK;
-      // A: thread t owns row t, 8 chunks of 8 k
-#pragma unroll 2
-      for (int c = 0; c < 8; ++c)
-        gather_chunk<T, P>(A, a_srow, a_sk, m0 + t, pr.m, k0, pr.k, st, Cfg::A_TILE, t, c);
-      // B: 64 rows x 8 chunks over 128 threads
-#pragma unroll 2
-      for (int c = (t >> 6) * 4; c < (t >> 6) * 4 + 4; ++c)
-        gather_chunk<T, P>(B, b_srow, b_sk, n0 + (t & 63), pr.n, k0, pr.k, st + P * Cfg::A_TILE, Cfg::B_TILE,
-                           t & 63, c);
+      ga.template store<P>(st, Cfg::A_TILE, t, 0);
+      gbt.template store<P>(st + P * Cfg::A_TILE, Cfg::B_TILE, t & 63, (t >> 6) * 4);
       fence_proxy_async_smem();
       tc::mbar_arrive(&full[s]);
       const bool chunk_end = (kb + 1 == nk) || ((kb + 1) % kGtChunk == 0);
