@@ -18,7 +18,6 @@
 
 #include "common.cuh"
 #include "reduce_util.cuh"
-#include "tc_ptx.cuh"
 
 namespace gb {
 
@@ -374,152 +373,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) blas1_reduce
 
 __global__ void fill_index(int32_t* result, int32_t v) { *result = v; }
 
-// ------------------------------------------------------ TMA-fed variant --
-// Long contiguous vectors: a producer warp streams 8 KB chunks (per array)
-// into a 6-stage shared-memory ring with 1-D bulk copies; chunk c goes to
-// CTA c mod grid, so each CTA walks its chunks in increasing index order and
-// the per-thread first-index rule of iamax/iamin still holds.  The elements
-// after the last whole chunk are read directly by the last CTA.  The bytes in
-// flight are set by the ring, not by registers.
-constexpr int kBsStages = 6;
-constexpr int kBsChunk = 8192;
-constexpr int kBsConsumers = 8;
-constexpr int kBsThreads = (kBsConsumers + 1) * 32;
-
-__device__ __forceinline__ void bulk_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          tc::smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(tc::smem_u32(bar))
-      : "memory");
-}
-
-enum : int { kErrStreamFull = 301, kErrStreamEmpty = 302, kErrStreamDrain = 303 };
-
-template <class Op, typename T, bool HAS_Y>
-__global__ void __launch_bounds__(kBsThreads) blas1_stream(int64_t n, const T* __restrict__ x,
-                                                           const T* __restrict__ y,
-                                                           typename Op::Acc* __restrict__ partials,
-                                                           unsigned int* __restrict__ ticket,
-                                                           typename Op::Out* __restrict__ result, int* err) {
-  using Acc = typename Op::Acc;
-  using V = Vec16<T>;
-  using VT = typename V::type;
-  constexpr int W = V::n;
-  constexpr int E = kBsChunk / int(sizeof(T));           // elements per chunk
-  constexpr int NA = HAS_Y ? 2 : 1;                       // arrays streamed
-  constexpr int VPT = E / (W * kBsConsumers * 32);        // 128-bit vectors per thread per chunk
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-  uint64_t* full = reinterpret_cast<uint64_t*>(ring + kBsStages * NA * kBsChunk);
-  uint64_t* empty = full + kBsStages;
-  __shared__ Acc smem[kBsThreads / 32];
-  __shared__ bool is_last;
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t nfull = n / E;
-  const int64_t G = gridDim.x;
-  const int my = nfull > int64_t(blockIdx.x) ? int((nfull - blockIdx.x + G - 1) / G) : 0;
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kBsStages; ++s) {
-      tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], kBsConsumers);
-    }
-    tc::fence_mbar_init();
-  }
-  __syncthreads();
-  Acc acc = Op::init();
-  if (warp == kBsConsumers) {
-    if (lane == 0) {
-      int issued = 0;
-      for (int i = 0; i < my; ++i) {
-        const int s = i % kBsStages;
-        if (!tc::mbar_wait(&empty[s], ((i / kBsStages) & 1) ^ 1)) {
-          atomicExch(err, kErrStreamEmpty);
-          break;
-        }
-        const int64_t c = blockIdx.x + int64_t(i) * G;
-        tc::mbar_arrive_expect_tx(&full[s], NA * kBsChunk);
-        bulk_load_1d(ring + (s * NA) * kBsChunk, x + c * E, kBsChunk, &full[s]);
-        if (HAS_Y) bulk_load_1d(ring + (s * NA + 1) * kBsChunk, y + c * E, kBsChunk, &full[s]);
-        issued = i + 1;
-      }
-      for (int i = issued > kBsStages ? issued - kBsStages : 0; i < issued; ++i)
-        if (!tc::mbar_wait(&full[i % kBsStages], (i / kBsStages) & 1)) {
-          atomicExch(err, kErrStreamDrain);
-          break;
-        }
-    }
-  } else {
-    const int t = threadIdx.x;
-    for (int i = 0; i < my; ++i) {
-      const int s = i % kBsStages;
-      if (!tc::mbar_wait(&full[s], (i / kBsStages) & 1)) {
-        if (lane == 0) atomicExch(err, kErrStreamFull);
-        break;
-      }
-      const int64_t base = (blockIdx.x + int64_t(i) * G) * E;
-      const VT* xs = reinterpret_cast<const VT*>(ring + (s * NA) * kBsChunk);
-      const VT* ys = reinterpret_cast<const VT*>(ring + (s * NA + (HAS_Y ? 1 : 0)) * kBsChunk);
-#pragma unroll
-      for (int j = 0; j < VPT; ++j) {
-        const int v = t + j * kBsConsumers * 32;
-        T xe[W], ye[W];
-        V::unpack(xs[v], xe);
-        if (HAS_Y) V::unpack(ys[v], ye);
-        Op::template add_vec<W>(acc, xe, HAS_Y ? ye : nullptr, base + int64_t(v) * W);
-      }
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&empty[s]);
-    }
-    if (blockIdx.x == gridDim.x - 1)
-      for (int64_t e = nfull * E + t; e < n; e += kBsConsumers * 32) Op::add(acc, x[e], HAS_Y ? y[e] : T(0), e);
-  }
-  acc = block_reduce<Op>(acc, smem);
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = acc;
-    __threadfence();
-    is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  Acc a = Op::init();
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) Op::combine(a, ldcg_any(partials + b));
-  __syncthreads();
-  a = block_reduce<Op>(a, smem);
-  if (threadIdx.x == 0) {
-    Op::finish(a, result);
-    *ticket = 0u;
-  }
-}
-
 // ------------------------------------------------------------------- host --
 template <class Op, typename T, bool HAS_Y>
 gbblas_status_t launch_reduce(gbblas_handle_t h, int64_t n, const T* x, int64_t incx, const T* y, int64_t incy,
                               typename Op::Out* result) {
   using Acc = typename Op::Acc;
   const bool vec = incx == 1 && aligned16(x) && (!HAS_Y || (incy == 1 && aligned16(y)));
-  constexpr int64_t E = kBsChunk / int64_t(sizeof(T));
-  if (vec && n >= 64 * E) {
-    // long contiguous vector: TMA-fed streaming
-    constexpr int NA = HAS_Y ? 2 : 1;
-    constexpr size_t smem = 128 + size_t(kBsStages) * NA * kBsChunk + 2 * kBsStages * 8;
-    const int per_sm = HAS_Y ? 2 : 4;
-    int64_t blocks = int64_t(h->sm_count) * per_sm;
-    if (blocks > n / E) blocks = n / E;
-    static bool attr = false;
-    if (!attr) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(blas1_stream<Op, T, HAS_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(smem)));
-      attr = true;
-    }
-    void* tmp = nullptr;
-    GB_TRY(temp_acquire(h, sizeof(Acc) * blocks, &tmp));
-    blas1_stream<Op, T, HAS_Y><<<unsigned(blocks), kBsThreads, smem, h->stream>>>(
-        n, x, y, static_cast<Acc*>(tmp), h->tickets, result, h->dev_error);
-    return after_launch("blas1_stream");
-  }
   const int64_t per_block = int64_t(kThreads) * (vec ? 16 / int(sizeof(T)) : 1) * kUnroll;
   int64_t blocks = cdiv(n > 0 ? n : 1, per_block);
   const int64_t cap = int64_t(h->sm_count) * (2048 / kThreads) * 1;
