@@ -55,7 +55,9 @@ gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g) {
     case GBBLAS_SGEMM_SPLIT_BF16X6: return launch_gemm_split_bf16(h, g, 3);
     default: break;
   }
-  // AUTO: every config is FP32-accurate; the selector picks one
+  // AUTO: many small problems go to the one-CTA-per-problem kernel; otherwise
+  // every config is FP32-accurate and the selector picks one
+  if (small_batched_applies(g, h->sm_count)) return launch_gemm_small_batched(h, g);
   gbblas_status_t s = launch_sgemm_config(h, g, select_sgemm_config(h, g));
   if (s != GBBLAS_STATUS_UNSUPPORTED) return s;
   clear_error();  // a config that cannot take this shape (grid / workspace limits)

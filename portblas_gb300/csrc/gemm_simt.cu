@@ -35,6 +35,80 @@ gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<double>& g) {
   return launch_simt_tile_128x128_f64(h, g, 1);
 }
 
+// ------------------------------------------------------ small batches --
+// Strided batches of small problems (M, N, K <= 64): one CTA per problem
+// loads all of A and B into shared memory in one coalesced pass (a single
+// wait instead of one per k-slab), each of 256 threads computes a 4x4 block,
+// and C goes back through shared memory so the stores are coalesced too.
+constexpr int kSmallMax = 64;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) gemm_small_batched_kernel(GemmArgs<float> g) {
+  __shared__ float As[kSmallMax][kSmallMax + 4];  // [k][i]
+  __shared__ float Bs[kSmallMax][kSmallMax + 4];  // [k][j]
+  const int64_t bz = blockIdx.x;
+  const float* A = g.a + bz * g.stride_a;
+  const float* B = g.b + bz * g.stride_b;
+  float* C = g.c + bz * g.stride_c;
+  const int M = int(g.m), N = int(g.n), K = int(g.k), t = threadIdx.x;
+  for (int e = t; e < M * K; e += 256) {
+    int i, k;
+    if (!TA) { i = e % M; k = e / M; } else { k = e % K; i = e / K; }
+    As[k][i] = TA ? A[k + int64_t(i) * g.lda] : A[i + int64_t(k) * g.lda];
+  }
+  for (int e = t; e < K * N; e += 256) {
+    int k, j;
+    if (!TB) { k = e % K; j = e / K; } else { j = e % N; k = e / N; }
+    Bs[k][j] = TB ? B[j + int64_t(k) * g.ldb] : B[k + int64_t(j) * g.ldb];
+  }
+  __syncthreads();
+  const int tx = t % 16, ty = t / 16;
+  float acc[4][4] = {};
+  for (int k = 0; k < K; ++k) {
+    float a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      a[q] = As[k][ty * 4 + q];
+      b[q] = Bs[k][tx * 4 + q];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+  }
+  __syncthreads();
+  // stage C in As as [j][i] for coalesced column-major stores
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) As[tx * 4 + j][ty * 4 + i] = acc[i][j];
+  __syncthreads();
+  for (int e = t; e < M * N; e += 256) {
+    const int i = e % M, j = e / M;
+    float* cp = C + i + int64_t(j) * g.ldc;
+    float v = g.alpha * As[j][i];
+    if (g.beta != 0.f) v = fmaf(g.beta, *cp, v);
+    *cp = v;
+  }
+}
+
+bool small_batched_applies(const GemmArgs<float>& g, int sm_count) {
+  return g.m <= kSmallMax && g.n <= kSmallMax && g.k <= kSmallMax && g.batch >= 4 * int64_t(sm_count) &&
+         g.batch <= INT32_MAX;
+}
+
+gbblas_status_t launch_gemm_small_batched(gbblas_handle_t h, const GemmArgs<float>& g) {
+  const dim3 grid(unsigned(g.batch));
+#define GB_SMALL(TA_, TB_) \
+  if (g.ta == TA_ && g.tb == TB_) gemm_small_batched_kernel<TA_, TB_><<<grid, 256, 0, h->stream>>>(g);
+  GB_SMALL(false, false)
+  GB_SMALL(false, true)
+  GB_SMALL(true, false)
+  GB_SMALL(true, true)
+#undef GB_SMALL
+  return after_launch("gemm_small_batched");
+}
+
 // ----------------------------------------------------------- interleaved --
 // gemm_batch_type_t::interleaved (src/operations/blas3/gemm_interleaved.hpp,
 // layout as in test/unittest/blas3/blas3_gemm_common.hpp:53-87): the batch

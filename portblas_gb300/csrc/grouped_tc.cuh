@@ -54,6 +54,17 @@ __device__ __forceinline__ float ld_f32<float>(const float* p) { return __ldg(p)
 template <>
 __device__ __forceinline__ float ld_f32<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 
+__device__ __forceinline__ void load_vec8(const float* p, float* v) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void load_vec8(const __nv_bfloat16* p, float* v) {
+  const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+  const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&a);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) v[e] = __bfloat162float(h[e]);
+}
+
 // Gathers NCH chunks of 8 consecutive k of one row (global row gr) of an
 // operand whose element (row, k) is at src[row*srow + k*sk]: load() issues
 // every global load of the k-block first (so they are all in flight
@@ -65,13 +76,29 @@ struct RowGather {
   __device__ __forceinline__ void load(const T* src, int64_t srow, int64_t sk, int64_t gr, int64_t rows, int64_t k0,
                                        int64_t K, int c0) {
     const bool row_ok = gr < rows;
-    const T* p = src + (row_ok ? gr : 0) * srow;
+    const T* p = src + (row_ok ? gr : 0) * srow + (k0 + int64_t(c0) * 8) * sk;
+    const int64_t kleft = K - (k0 + int64_t(c0) * 8);  // valid k from the first chunk on
+    if (row_ok && kleft >= NCH * 8) {
+      if (sk == 1 && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+        // K contiguous and 16-byte aligned: 128-bit loads
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) load_vec8(p + c * 8, v[c]);
+      } else {
+        // interior: no per-element bounds checks, 32-bit strides
+        const int s = int(sk);
+#pragma unroll
+        for (int c = 0; c < NCH; ++c)
+#pragma unroll
+          for (int e = 0; e < 8; ++e) v[c][e] = ld_f32<T>(p + (c * 8 + e) * s);
+      }
+      return;
+    }
 #pragma unroll
     for (int c = 0; c < NCH; ++c)
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
-        const int64_t kk = k0 + (c0 + c) * 8 + e;
-        v[c][e] = (row_ok && kk < K) ? ld_f32<T>(p + kk * sk) : 0.f;
+        const int64_t kk = int64_t(c) * 8 + e;
+        v[c][e] = (row_ok && kk < kleft) ? ld_f32<T>(p + kk * sk) : 0.f;
       }
   }
   template <int P>

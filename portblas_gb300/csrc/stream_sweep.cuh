@@ -30,6 +30,8 @@ enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203 };
 
 // x elements staged in shared memory by the rows sweep (one column split)
 constexpr int64_t kRowsXStage = 8192;
+// rows per chunk of the cols sweep when x is staged (8 KB of FP32 x)
+constexpr int64_t kColsXRows = 2048;
 
 // barrier among the 8 consumer warps only (the producer keeps streaming)
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -365,15 +367,16 @@ inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes)
 }
 
 // cols sweep: rows split into chunks (a multiple of the 1 KB tile; with x
-// at most 4096 rows so the chunk of x fits in shared memory), then each CTA
+// at most kColsXRows rows so the chunk of x fits in shared memory), then each CTA
 // takes `ctiles` column tiles so the grid is about one wave of resident CTAs.
 inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes, bool has_x) {
   const int64_t BR = 1024 / elem_bytes, BC = kStTileBytes / 1024;
-  const int64_t slots = int64_t(sm_count) * (has_x ? 2 : 3);
+  // 3 resident CTAs per SM: the 64 KB ring plus at most 8 KB of x
+  const int64_t slots = int64_t(sm_count) * 3;
   TmaPlan p;
   const int64_t coltiles = cdiv(N, BC);
   int64_t split = slots / coltiles;
-  const int64_t min_split = has_x ? cdiv(M, 4096) : 1;
+  const int64_t min_split = has_x ? cdiv(M, kColsXRows) : 1;
   const int64_t max_split = cdiv(M, 4 * BR);
   if (split > max_split) split = max_split;
   if (split < min_split) split = min_split;
@@ -447,7 +450,7 @@ inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(cols_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(cols_tma_smem<T>(HAS_X, 4096)));
+                         int(cols_tma_smem<T>(HAS_X, kColsXRows)));
     attr = true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));

@@ -262,3 +262,31 @@ def test_gemm_batched_interleaved(sb, torch_cuda, ta, tb, m, n, k, batch, alpha,
     for i in range(0, batch, max(1, batch // 7)):
         ref = oracle.gemm(ta, tb, m, n, k, alpha, As[i], lda, Bs[i], ldb, beta, Cs[i], ldc)
         assert_almost_equal(out[i].reshape(n, ldc).T[:m], ref)
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("m,n,k", [(64, 64, 64), (7, 33, 64), (64, 1, 17), (50, 60, 3)])
+@pytest.mark.parametrize("beta", [0.0, 0.75])
+def test_gemm_strided_small_batch_path(sb, torch_cuda, ta, tb, m, n, k, beta):
+    """Many small problems take the one-CTA-per-problem kernel under AUTO."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    g = rng(m * n + k)
+    batch = 700
+    lda, ldb, ldc = (k if ta else m) + 1, (n if tb else k) + 2, m + 3
+    sa, sbs, sc = lda * (m if ta else k) + 5, ldb * (k if tb else n), ldc * n + 1
+    a = g.uniform(-1, 1, sa * batch).astype(np.float32)
+    b = g.uniform(-1, 1, sbs * batch).astype(np.float32)
+    c = g.uniform(-1, 1, sc * batch).astype(np.float32)
+    cd = to_dev(c, torch)
+    blas._gemm_strided_batched(sb, "t" if ta else "n", "t" if tb else "n", m, n, k, 1.25, to_dev(a, torch), lda, sa,
+                               to_dev(b, torch), ldb, sbs, beta, cd, ldc, sc, batch)
+    out = to_host(cd)
+    for i in (0, 1, 350, batch - 1):
+        ref = oracle.gemm(ta, tb, m, n, k, 1.25, a[i * sa:], lda, b[i * sbs:], ldb, beta, c[i * sc:], ldc)
+        got = out[i * sc:i * sc + ldc * n].reshape(n, ldc).T[:m]
+        assert_almost_equal(got, ref)
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * k)
+        np.testing.assert_array_equal(out[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:],
+                                      c[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:])
