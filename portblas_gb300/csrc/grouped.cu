@@ -260,7 +260,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
 
 static int grouped_grid(gbblas_handle_t h, int64_t tiles, int method, int dtype) {
   // resident CTAs per SM: SIMT 8 x 256 threads; tcgen05 by shared memory
-  const int per_sm = method == 0 ? 8 : (dtype == GBBLAS_DTYPE_BF16 ? 4 : 1);
+  const int per_sm = method == 0 ? 8 : (dtype == GBBLAS_DTYPE_BF16 ? 2 : 1);
   const int64_t cap = int64_t(h->sm_count) * per_sm;
   return int(std::max<int64_t>(1, std::min<int64_t>(tiles, cap)));
 }

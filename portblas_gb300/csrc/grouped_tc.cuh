@@ -13,10 +13,11 @@
 // stores to the tensor core before the stage's mbarrier arrival.
 //
 // Per k-block (64) and stage: P A-term tiles (128 x 64) and P B-term tiles
-// (64 x 64); two stages.  Thread 0 issues the MMAs (all term pairs with
-// a + b <= P - 1) and commits each stage back to the loaders.  Every 8
-// k-blocks the TMEM accumulator is promoted into FP32 registers (one output
-// row of 64 columns per thread) so long K keeps FP32-level accuracy.
+// (64 x 64); two stages; 256 threads gather.  Thread 0 issues the MMAs (all
+// term pairs with a + b <= P - 1) and commits each stage back to the loaders.
+// Every 8 k-blocks the TMEM accumulator is promoted into FP32 registers (warp
+// w holds rows 32*(w%4).. and 32 of the 64 columns) so long K keeps
+// FP32-level accuracy.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -25,7 +26,7 @@
 
 namespace gb {
 
-constexpr int kGtBM = 128, kGtBN = 64, kGtBK = 64, kGtThreads = 128, kGtChunk = 8;
+constexpr int kGtBM = 128, kGtBN = 64, kGtBK = 64, kGtThreads = 256, kGtChunk = 8;
 
 template <int P>
 struct GtCfg {
@@ -125,7 +126,7 @@ enum : int { kErrGtFull = 401, kErrGtEmpty = 402, kErrGtAcc = 403 };
 // probs / count / total_tiles / counters: as grouped_gemm_kernel (grouped.cu),
 // with tiles of 128 x 64.
 template <typename T, int P, class Prob>
-__global__ void __launch_bounds__(kGtThreads, 1)
+__global__ void __launch_bounds__(kGtThreads, 2)
     grouped_tc_kernel(const Prob* __restrict__ probs, int count, int64_t total_tiles,
                       unsigned long long* __restrict__ counters, int* __restrict__ err) {
   using Cfg = GtCfg<P>;
@@ -185,29 +186,32 @@ __global__ void __launch_bounds__(kGtThreads, 1)
     const int64_t a_srow = pr.ta ? pr.lda : 1, a_sk = pr.ta ? 1 : pr.lda;
     const int64_t b_srow = pr.tb ? 1 : pr.ldb, b_sk = pr.tb ? pr.ldb : 1;
     const int nk = int((pr.k + kGtBK - 1) / kGtBK);
-    float sum[kGtBN];
+    // warp w: TMEM lanes 32*(w%4) (rows), columns 32*(w/4) .. +31 of the tile
+    const int half = warp >> 2;
+    float sum[kGtBN / 2];
 #pragma unroll
-    for (int i = 0; i < kGtBN; ++i) sum[i] = 0.f;
-    RowGather<T, 8> ga;
-    RowGather<T, 4> gbt;
+    for (int i = 0; i < kGtBN / 2; ++i) sum[i] = 0.f;
+    RowGather<T, 4> ga;
+    RowGather<T, 2> gbt;
     bool ok = true;
     for (int kb = 0; kb < nk && ok; ++kb, ++it) {
       const int s = it % Cfg::STAGES;
       const uint32_t ph = (it / Cfg::STAGES) & 1;
       uint8_t* st = smem + s * Cfg::STAGE;
       const int64_t k0 = int64_t(kb) * kGtBK;
-      // A: thread t owns row t (8 chunks); B: 64 rows x 8 chunks over 128 threads.
+      // A: 128 rows x 8 chunks, thread t takes row t%128, chunks 4*(t/128)..+3;
+      // B: 64 rows x 8 chunks, thread t takes row t%64, chunks 2*(t/64)..+1.
       // The loads go out before the wait for the stage, overlapping the MMAs
       // still reading it.
-      ga.load(A, a_srow, a_sk, m0 + t, pr.m, k0, pr.k, 0);
-      gbt.load(B, b_srow, b_sk, n0 + (t & 63), pr.n, k0, pr.k, (t >> 6) * 4);
+      ga.load(A, a_srow, a_sk, m0 + (t & 127), pr.m, k0, pr.k, (t >> 7) * 4);
+      gbt.load(B, b_srow, b_sk, n0 + (t & 63), pr.n, k0, pr.k, (t >> 6) * 2);
       if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
         if (t == 0) atomicExch(err, kErrGtEmpty);
         ok = false;
         break;
       }
-      ga.template store<P>(st, Cfg::A_TILE, t, 0);
-      gbt.template store<P>(st + P * Cfg::A_TILE, Cfg::B_TILE, t & 63, (t >> 6) * 4);
+      ga.template store<P>(st, Cfg::A_TILE, t & 127, (t >> 7) * 4);
+      gbt.template store<P>(st + P * Cfg::A_TILE, Cfg::B_TILE, t & 63, (t >> 6) * 2);
       fence_proxy_async_smem();
       tc::mbar_arrive(&full[s]);
       const bool chunk_end = (kb + 1 == nk) || ((kb + 1) % kGtChunk == 0);
@@ -240,14 +244,11 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         ++nacc;
         tc::tc_fence_after();
         if (ok) {
+          uint32_t r[32];
+          tc::tmem_ld_32x32b_x32(tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(half * 32), r);
+          tc::tmem_ld_wait();
 #pragma unroll
-          for (int c0 = 0; c0 < kGtBN; c0 += 32) {
-            uint32_t r[32];
-            tc::tmem_ld_32x32b_x32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), r);
-            tc::tmem_ld_wait();
-#pragma unroll
-            for (int i = 0; i < 32; ++i) sum[c0 + i] += __uint_as_float(r[i]);
-          }
+          for (int i = 0; i < 32; ++i) sum[i] += __uint_as_float(r[i]);
         }
         tc::tc_fence_before();
         __syncthreads();  // everyone has read TMEM before the next chunk's MMAs
@@ -259,12 +260,12 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       __syncthreads();
       break;
     }
-    // epilogue: thread t owns row m0 + t (TMEM lane t)
-    const int64_t gm = m0 + t;
+    // epilogue: row m0 + 32*(warp%4) + lane, columns n0 + 32*half + i
+    const int64_t gm = m0 + (warp & 3) * 32 + (t & 31);
     if (gm < pr.m) {
 #pragma unroll
-      for (int i = 0; i < kGtBN; ++i) {
-        const int64_t gn = n0 + i;
+      for (int i = 0; i < kGtBN / 2; ++i) {
+        const int64_t gn = n0 + half * 32 + i;
         if (gn < pr.n) {
           float* cp = pr.c + gm + gn * pr.ldc;
           float v = pr.alpha * sum[i];
