@@ -30,8 +30,8 @@ enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203 };
 
 // x elements staged in shared memory by the rows sweep (one column split)
 constexpr int64_t kRowsXStage = 8192;
-// rows per chunk of the cols sweep when x is staged (8 KB of FP32 x)
-constexpr int64_t kColsXRows = 2048;
+// rows per chunk of the cols sweep when x is staged (16 KB of FP32 x)
+constexpr int64_t kColsXRows = 4096;
 
 // barrier among the 8 consumer warps only (the producer keeps streaming)
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -371,8 +371,8 @@ inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes)
 // takes `ctiles` column tiles so the grid is about one wave of resident CTAs.
 inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes, bool has_x) {
   const int64_t BR = 1024 / elem_bytes, BC = kStTileBytes / 1024;
-  // 3 resident CTAs per SM: the 64 KB ring plus at most 8 KB of x
-  const int64_t slots = int64_t(sm_count) * 3;
+  // resident CTAs per SM: 3 with the 64 KB ring alone, 2 with 16 KB of x
+  const int64_t slots = int64_t(sm_count) * (has_x ? 2 : 3);
   TmaPlan p;
   const int64_t coltiles = cdiv(N, BC);
   int64_t split = slots / coltiles;
