@@ -151,6 +151,24 @@ gbblas_status_t gbblas_idamax_sync(gbblas_handle_t h, int64_t n, const double* x
 gbblas_status_t gbblas_idamin_sync(gbblas_handle_t h, int64_t n, const double* x, int64_t incx,
                                    int32_t* host_result);
 
+/* Element-wise BLAS-1 neighbours of the hot path (the GEMM alpha == 0
+ * shortcut uses the same scaling rule):
+ *   _scal  include/interface/blas1_interface.h:697-701  x <- alpha*x (alpha == 0 writes zeros)
+ *   _axpy  include/interface/blas1_interface.h:536-541  y <- alpha*x + y
+ *   _copy  include/interface/blas1_interface.h:556-560  y <- x
+ *   _sdsdot include/interface/blas1_interface.h:615-620 result <- sb + dot(x, y) (n == 0: sb) */
+gbblas_status_t gbblas_sscal(gbblas_handle_t h, int64_t n, float alpha, float* x, int64_t incx);
+gbblas_status_t gbblas_dscal(gbblas_handle_t h, int64_t n, double alpha, double* x, int64_t incx);
+gbblas_status_t gbblas_saxpy(gbblas_handle_t h, int64_t n, float alpha, const float* x, int64_t incx, float* y,
+                             int64_t incy);
+gbblas_status_t gbblas_daxpy(gbblas_handle_t h, int64_t n, double alpha, const double* x, int64_t incx, double* y,
+                             int64_t incy);
+gbblas_status_t gbblas_scopy(gbblas_handle_t h, int64_t n, const float* x, int64_t incx, float* y, int64_t incy);
+gbblas_status_t gbblas_dcopy(gbblas_handle_t h, int64_t n, const double* x, int64_t incx, double* y,
+                             int64_t incy);
+gbblas_status_t gbblas_sdsdot(gbblas_handle_t h, int64_t n, float sb, const float* x, int64_t incx, const float* y,
+                              int64_t incy, float* result);
+
 /* ---------------------------------------------------------------- BLAS-2 -- */
 /* blas::_gemv  (include/interface/blas2_interface.h:632-655;
  *   src/interface/blas2_interface.hpp:68-217, 1163-1192).
@@ -214,6 +232,16 @@ gbblas_status_t gbblas_dgemm_strided_batched(gbblas_handle_t h, char transa, cha
                                              int64_t stride_a, const double* b, int64_t ldb, int64_t stride_b,
                                              double beta, double* c, int64_t ldc, int64_t stride_c,
                                              int64_t batch_size);
+
+/* blas::_symm (include/interface/blas3_interface.h:135-145): C <- alpha*A*B +
+ * beta*C (side 'l', A m x m) or alpha*B*A + beta*C (side 'r', A n x n), A
+ * symmetric with only the `uplo` ('u'/'l') triangle referenced. */
+gbblas_status_t gbblas_ssymm(gbblas_handle_t h, char side, char uplo, int64_t m, int64_t n, float alpha,
+                             const float* a, int64_t lda, const float* b, int64_t ldb, float beta, float* c,
+                             int64_t ldc);
+gbblas_status_t gbblas_dsymm(gbblas_handle_t h, char side, char uplo, int64_t m, int64_t n, double alpha,
+                             const double* a, int64_t lda, const double* b, int64_t ldb, double beta, double* c,
+                             int64_t ldc);
 
 /* FP32 GEMM tile configurations (no portBLAS counterpart: portBLAS fixes its
  * tile at compile time from size thresholds,
@@ -292,6 +320,20 @@ gbblas_status_t gbblas_grouped_plan_run(gbblas_handle_t h, gbblas_grouped_plan_t
 gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t plan);
 
 /* ------------------------------------------------------------ extension -- */
+/* blas::extension::_omatcopy (include/interface/extension_interface.h:188-198):
+ * out <- alpha * op(in); in is m x n, out is m x n ('n') or n x m ('t'/'c'). */
+gbblas_status_t gbblas_somatcopy(gbblas_handle_t h, char trans, int64_t m, int64_t n, float alpha, const float* in,
+                                 int64_t ld_in, float* out, int64_t ld_out);
+gbblas_status_t gbblas_domatcopy(gbblas_handle_t h, char trans, int64_t m, int64_t n, double alpha,
+                                 const double* in, int64_t ld_in, double* out, int64_t ld_out);
+/* blas::extension::_transpose (include/interface/extension_interface.h:405-452):
+ * out of place B <- A^T (A m x n), and in place (A reinterpreted from ld_in to
+ * its n x m transpose with ld_out, through temp memory). */
+gbblas_status_t gbblas_stranspose(gbblas_handle_t h, int64_t m, int64_t n, const float* a, int64_t ld_a, float* b,
+                                  int64_t ld_b);
+gbblas_status_t gbblas_stranspose_inplace(gbblas_handle_t h, int64_t m, int64_t n, float* a, int64_t ld_in,
+                                          int64_t ld_out);
+
 /* blas::extension::_reduction<op, T> (include/interface/extension_interface.h:453-462;
  *   src/interface/extension_interface.hpp:344-409, 578-593;
  *   src/operations/extension/reduction.hpp:35-236).

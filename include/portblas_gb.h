@@ -171,6 +171,22 @@ typename sb_handle_t::event_t _gemm_strided_batched(sb_handle_t& sb, char ta, ch
     throw unsupported_exception("_gemm_strided_batched: element type not supported");
 }
 
+/* _symm: include/interface/blas3_interface.h:135-145 */
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename container_2_t,
+          typename element_t, typename index_t>
+typename sb_handle_t::event_t _symm(sb_handle_t& sb, char side, char uplo, index_t M, index_t N, element_t alpha,
+                                    container_0_t a, index_t lda, container_1_t b, index_t ldb, element_t beta,
+                                    container_2_t c, index_t ldc, const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_2_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_ssymm(sb.native(), side, uplo, M, N, float(alpha), a, lda, b, ldb, float(beta), c, ldc));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dsymm(sb.native(), side, uplo, M, N, double(alpha), a, lda, b, ldb, double(beta), c, ldc));
+  else
+    throw unsupported_exception("_symm: element type not supported");
+}
+
 /* ------------------------------------------------------------------ BLAS-2 */
 template <typename sb_handle_t, typename index_t, typename element_t, typename container_t0,
           typename container_t1, typename increment_t, typename container_t2>
@@ -291,8 +307,113 @@ PORTBLAS_GB_IAM(_iamax, gbblas_isamax, gbblas_idamax)
 PORTBLAS_GB_IAM(_iamin, gbblas_isamin, gbblas_idamin)
 #undef PORTBLAS_GB_IAM
 
+/* _scal: include/interface/blas1_interface.h:697-701 */
+template <typename sb_handle_t, typename element_t, typename container_0_t, typename index_t,
+          typename increment_t>
+typename sb_handle_t::event_t _scal(sb_handle_t& sb, index_t N, element_t alpha, container_0_t x, increment_t incx,
+                                    const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_0_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_sscal(sb.native(), N, float(alpha), x, incx));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dscal(sb.native(), N, double(alpha), x, incx));
+  else
+    throw unsupported_exception("_scal: element type not supported");
+}
+
+/* _axpy: include/interface/blas1_interface.h:536-541 */
+template <typename sb_handle_t, typename element_t, typename container_0_t, typename container_1_t,
+          typename index_t, typename increment_t>
+typename sb_handle_t::event_t _axpy(sb_handle_t& sb, index_t N, element_t alpha, container_0_t x, increment_t incx,
+                                    container_1_t y, increment_t incy,
+                                    const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_1_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_saxpy(sb.native(), N, float(alpha), x, incx, y, incy));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_daxpy(sb.native(), N, double(alpha), x, incx, y, incy));
+  else
+    throw unsupported_exception("_axpy: element type not supported");
+}
+
+/* _copy: include/interface/blas1_interface.h:556-560 */
+template <typename sb_handle_t, typename index_t, typename container_0_t, typename increment_t,
+          typename container_1_t>
+typename sb_handle_t::event_t _copy(sb_handle_t& sb, index_t N, container_0_t x, increment_t incx, container_1_t y,
+                                    increment_t incy, const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<container_1_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_scopy(sb.native(), N, x, incx, y, incy));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_dcopy(sb.native(), N, x, incx, y, incy));
+  else
+    throw unsupported_exception("_copy: element type not supported");
+}
+
+/* _sdsdot: include/interface/blas1_interface.h:615-620 (async), :935-940 (sync) */
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename container_2_t,
+          typename index_t, typename increment_t>
+typename sb_handle_t::event_t _sdsdot(sb_handle_t& sb, index_t N, float sbv, container_0_t x, increment_t incx,
+                                      container_1_t y, increment_t incy, container_2_t rs,
+                                      const typename sb_handle_t::event_t& deps = {}) {
+  sb.depend(deps);
+  return sb.done(gbblas_sdsdot(sb.native(), N, sbv, x, incx, y, incy, rs));
+}
+template <typename sb_handle_t, typename container_0_t, typename container_1_t, typename index_t,
+          typename increment_t>
+float _sdsdot(sb_handle_t& sb, index_t N, float sbv, container_0_t x, increment_t incx, container_1_t y,
+              increment_t incy, const typename sb_handle_t::event_t& deps = {}) {
+  sb.depend(deps);
+  float* d = nullptr;
+  if (cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(float), sb.get_queue()) != cudaSuccess)
+    throw std::runtime_error("_sdsdot: device allocation failed");
+  gbblas_status_t st = gbblas_sdsdot(sb.native(), N, sbv, x, incx, y, incy, d);
+  float r = 0.f;
+  if (st == GBBLAS_STATUS_SUCCESS)
+    cudaMemcpyAsync(&r, d, sizeof(float), cudaMemcpyDeviceToHost, sb.get_queue());
+  cudaFreeAsync(d, sb.get_queue());
+  cudaStreamSynchronize(sb.get_queue());
+  detail::check(st);
+  return r;
+}
+
 /* --------------------------------------------------------------- extension */
 namespace extension {
+/* _omatcopy: include/interface/extension_interface.h:188-198 */
+template <typename sb_handle_t, typename element_t, typename index_t, typename in_t, typename out_t>
+typename sb_handle_t::event_t _omatcopy(sb_handle_t& sb, char trans, index_t m, index_t n, element_t alpha,
+                                        in_t in_memory, index_t ld_in, out_t out_memory, index_t ld_out,
+                                        const typename sb_handle_t::event_t& deps = {}) {
+  using T = detail::elem_t<out_t>;
+  sb.depend(deps);
+  if constexpr (std::is_same_v<T, float>)
+    return sb.done(gbblas_somatcopy(sb.native(), trans, m, n, float(alpha), in_memory, ld_in, out_memory, ld_out));
+  else if constexpr (std::is_same_v<T, double>)
+    return sb.done(gbblas_domatcopy(sb.native(), trans, m, n, double(alpha), in_memory, ld_in, out_memory, ld_out));
+  else
+    throw unsupported_exception("_omatcopy: element type not supported");
+}
+
+/* _transpose in place: include/interface/extension_interface.h:416-423 */
+template <typename element_t, typename sb_handle_t, typename index_t, typename in_t>
+typename sb_handle_t::event_t _transpose(sb_handle_t& sb, index_t m, index_t n, in_t A, index_t ld_in, index_t ld_out,
+                                         const typename sb_handle_t::event_t& deps = {}) {
+  static_assert(std::is_same_v<element_t, float>, "_transpose: element type not supported");
+  sb.depend(deps);
+  return sb.done(gbblas_stranspose_inplace(sb.native(), m, n, A, ld_in, ld_out));
+}
+
+/* _transpose out of place: include/interface/extension_interface.h:443-450 */
+template <typename element_t, typename sb_handle_t, typename index_t, typename in_t, typename out_t>
+typename sb_handle_t::event_t _transpose(sb_handle_t& sb, index_t m, index_t n, in_t A, index_t ld_a, out_t B,
+                                         index_t ld_b, const typename sb_handle_t::event_t& deps = {}) {
+  static_assert(std::is_same_v<element_t, float>, "_transpose: element type not supported");
+  sb.depend(deps);
+  return sb.done(gbblas_stranspose(sb.native(), m, n, A, ld_a, B, ld_b));
+}
 /* include/interface/extension_interface.h:453-462 */
 template <typename operator_t, typename element_t, typename sb_handle_t, typename input_t, typename output_t,
           typename index_t>

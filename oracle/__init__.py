@@ -179,6 +179,69 @@ def iamin(n, x, incx, dtype=np.float32) -> int:
     return int(lib().orc_iamax(n, _p(_f64(x)), incx, 0, _tmax(dtype)))
 
 
+# ------------------------------------------------ element-wise BLAS-1 --
+def scal(n, alpha, x, incx):
+    """x <- alpha*x; alpha == 0 writes zeros (src/interface/blas1_interface.hpp:438-455).
+    Returns the whole updated buffer."""
+    out = np.array(x, dtype=np.float64, copy=True)
+    idx = np.arange(n, dtype=np.int64)
+    pos = idx * incx if incx >= 0 else (n - 1 - idx) * (-incx)
+    out[pos] = 0.0 if alpha == 0 else alpha * out[pos]
+    return out
+
+
+def axpy(n, alpha, x, incx, y, incy):
+    """y <- alpha*x + y on strided views; returns the whole updated y."""
+    out = np.array(y, dtype=np.float64, copy=True)
+    idx = np.arange(n, dtype=np.int64)
+    py = idx * incy if incy >= 0 else (n - 1 - idx) * (-incy)
+    out[py] = alpha * view(x, n, incx) + out[py]
+    return out
+
+
+def copy(n, x, incx, y, incy):
+    out = np.array(y, dtype=np.float64, copy=True)
+    idx = np.arange(n, dtype=np.int64)
+    py = idx * incy if incy >= 0 else (n - 1 - idx) * (-incy)
+    out[py] = view(x, n, incx)
+    return out
+
+
+def sdsdot(n, sb, x, incx, y, incy):
+    """sb + dot(x, y); n == 0 gives sb (src/interface/blas1_interface.hpp:150-177)."""
+    return float(sb) + (dot(n, x, incx, y, incy) if n > 0 else 0.0)
+
+
+def omatcopy(trans, m, n, alpha, a, ld_in, out, ld_out):
+    """out <- alpha*op(in) (include/interface/extension_interface.h:175-198);
+    returns the whole updated out buffer."""
+    A = np.asarray(a, dtype=np.float64)
+    res = np.array(out, dtype=np.float64, copy=True)
+    for j in range(n):
+        col = alpha * A[j * ld_in: j * ld_in + m]
+        if trans in ("n", "N"):
+            res[j * ld_out: j * ld_out + m] = col
+        else:
+            res[j + np.arange(m) * ld_out] = col
+    return res
+
+
+def symm(side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc):
+    """SYMM from the referenced triangle of A (one triangle mirrored), then
+    the double-double GEMM oracle (m x n result, Fortran order)."""
+    na = m if side in ("l", "L") else n
+    A = np.asarray(a, dtype=np.float64)
+    full = np.empty((na, na))
+    for j in range(na):
+        for i in range(na):
+            direct = (i <= j) if uplo in ("u", "U") else (i >= j)
+            full[i, j] = A[i + j * lda] if direct else A[j + i * lda]
+    F = full.ravel(order="F")
+    if side in ("l", "L"):
+        return gemm(False, False, m, n, m, alpha, F, na, b, ldb, beta, c, ldc)
+    return gemm(False, False, m, n, n, alpha, b, ldb, F, na, beta, c, ldc)
+
+
 # ---------------------------------------------------------- reduction --
 OPS = {"add": 0, "product": 1, "max": 2, "min": 3, "abs_add": 4, "mean": 5}
 DIMS = {"inner": 0, "outer": 1}

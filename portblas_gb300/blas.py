@@ -282,9 +282,62 @@ def _iamin(sb_handle, N, x, incx, rs=None, dependencies=None, dtype=None):
     return out.value
 
 
+def _scal(sb_handle, N, alpha, x, incx, dependencies=None, dtype=None):
+    """blas::_scal (include/interface/blas1_interface.h:697-701)."""
+    p = _prefix(x, dtype)
+    return _call(f"gbblas_{p}scal", sb_handle.handle, N, alpha, _ptr(x), incx)
+
+
+def _axpy(sb_handle, N, alpha, x, incx, y, incy, dependencies=None, dtype=None):
+    """blas::_axpy (include/interface/blas1_interface.h:536-541)."""
+    p = _prefix(y, dtype)
+    return _call(f"gbblas_{p}axpy", sb_handle.handle, N, alpha, _ptr(x), incx, _ptr(y), incy)
+
+
+def _copy(sb_handle, N, x, incx, y, incy, dependencies=None, dtype=None):
+    """blas::_copy (include/interface/blas1_interface.h:556-560)."""
+    p = _prefix(y, dtype)
+    return _call(f"gbblas_{p}copy", sb_handle.handle, N, _ptr(x), incx, _ptr(y), incy)
+
+
+def _sdsdot(sb_handle, N, sb, x, incx, y, incy, rs=None, dependencies=None):
+    """blas::_sdsdot: async with ``rs`` (blas1_interface.h:615-620), sync without."""
+    if rs is not None:
+        return _call("gbblas_sdsdot", sb_handle.handle, N, sb, _ptr(x), incx, _ptr(y), incy, _ptr(rs))
+    import torch
+    r = torch.empty(1, dtype=torch.float32, device="cuda")
+    _call("gbblas_sdsdot", sb_handle.handle, N, sb, _ptr(x), incx, _ptr(y), incy, _ptr(r))
+    return float(r.item())
+
+
+def _symm(sb_handle, side, uplo, M, N, alpha, a, lda, b, ldb, beta, c, ldc, dependencies=None, dtype=None):
+    """blas::_symm (include/interface/blas3_interface.h:135-145)."""
+    p = _prefix(c, dtype)
+    return _call(f"gbblas_{p}symm", sb_handle.handle, _ch(side), _ch(uplo), M, N, alpha, _ptr(a), lda, _ptr(b), ldb,
+                 beta, _ptr(c), ldc)
+
+
 # ---------------------------------------------------------- extension --
 class extension:
     """blas::extension namespace."""
+
+    @staticmethod
+    def _omatcopy(sb_handle, trans, m, n, alpha, in_memory, ld_in, out_memory, ld_out, dependencies=None,
+                  dtype=None):
+        """blas::extension::_omatcopy (include/interface/extension_interface.h:188-198)."""
+        p = _prefix(in_memory, dtype)
+        return _call(f"gbblas_{p}omatcopy", sb_handle.handle, _ch(trans), m, n, alpha, _ptr(in_memory), ld_in,
+                     _ptr(out_memory), ld_out)
+
+    @staticmethod
+    def _transpose(sb_handle, m, n, A, ld_a, B=None, ld_b=None, dependencies=None):
+        """blas::extension::_transpose: out of place (A -> B, ld_b) or, with
+        B omitted and ld_b the output leading dimension, in place
+        (include/interface/extension_interface.h:405-452)."""
+        if B is None or isinstance(B, int) and ld_b is None:
+            ld_out = B if ld_b is None else ld_b
+            return _call("gbblas_stranspose_inplace", sb_handle.handle, m, n, _ptr(A), ld_a, ld_out)
+        return _call("gbblas_stranspose", sb_handle.handle, m, n, _ptr(A), ld_a, _ptr(B), ld_b)
 
     @staticmethod
     def _reduction(operator_t, sb_handle, buffer_in, ld, buffer_out, rows, cols, reduction_dim,
