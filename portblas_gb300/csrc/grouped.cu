@@ -6,13 +6,14 @@
 // src/operations/blas3/gemm_local.hpp:438-516); each problem here keeps the
 // blas::_gemm semantics (alpha/beta rules, any transposes, column-major).
 //
-// Scheduler: the problems' 64x64 output tiles are numbered in problem order
-// (prefix sums of per-problem tile counts in the device problem table).
-// Every CTA of a persistent grid (a multiple of the SM count) takes the next
-// tile number from a global atomic counter, finds its problem by binary
-// search, and computes the tile; no CTA ever waits on another.  The last CTA
-// to finish resets the counters, so the same launch can be replayed from a
-// CUDA graph with no host work.
+// Scheduler: the problems are ordered by decreasing k (longest tiles first,
+// so the dynamic schedule ends balanced) and their output tiles numbered in
+// that order (prefix sums of per-problem tile counts in the device problem
+// table; a tile -> problem table beside it).  Every CTA of a persistent grid
+// (a multiple of the SM count) takes the next tile number from a global
+// atomic counter, finds its problem, and computes the tile; no CTA ever waits
+// on another.  The last CTA to finish resets the counters, so the same launch
+// can be replayed from a CUDA graph with no host work.
 //
 // Tile compute: A and B slabs (BK = 16) are converted from FP32 or BF16 to
 // FP32 as they are staged in shared memory (any transpose), and each of 256
@@ -23,12 +24,18 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "gemm_internal.cuh"
 #include "grouped_tc.cuh"
 
 namespace gb {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder();  // gemm_tc.cu
 
 struct GroupedProblem {
   int m, n, k;
@@ -150,16 +157,23 @@ __global__ void __launch_bounds__(kGThreads) grouped_gemm_kernel(const GroupedPr
 
 }  // namespace gb
 
-// A grouped plan: the device problem table, the scheduler counters and the
-// instantiated CUDA graph of the persistent launch.
+// A grouped plan: one device block holding the problem table, the tile ->
+// problem table, the scheduler counters and (tcgen05 path) the operand tensor
+// maps, the operand conversion list and the BF16 terms; plus the instantiated
+// CUDA graph of the launch.
 struct gbblas_grouped_plan_s {
   int dtype = 0;
   int method = 1;  // 1: tcgen05 tiles (128 x 64), 0: SIMT tiles (64 x 64)
   int count = 0;
   int64_t total_tiles = 0;
   int grid = 0;
+  void* block = nullptr;  // owned device block (plans only)
   gb::GroupedProblem* table = nullptr;
+  int* tile_prob = nullptr;
   unsigned long long* counters = nullptr;
+  CUtensorMap* maps = nullptr;
+  gb::GtOperand* ops = nullptr;
+  int n_ops = 0;
   cudaGraphExec_t exec = nullptr;
   int device = 0;
   int* err = nullptr;  // device error word of the creating handle
@@ -167,29 +181,27 @@ struct gbblas_grouped_plan_s {
 
 using namespace gb;
 
-static gbblas_status_t launch_grouped(cudaStream_t s, gbblas_grouped_plan_s* p, int* err) {
-  if (p->method == 1) {
-    if (p->dtype == GBBLAS_DTYPE_BF16) {
-      static bool attr = false;
-      if (!attr) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<__nv_bfloat16, 1, GroupedProblem>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<1>::SMEM));
-        attr = true;
-      }
-      grouped_tc_kernel<__nv_bfloat16, 1, GroupedProblem><<<p->grid, kGtThreads, GtCfg<1>::SMEM, s>>>(
-          p->table, p->count, p->total_tiles, p->counters, err);
-    } else {
-      static bool attr = false;
-      if (!attr) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<float, 3, GroupedProblem>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<3>::SMEM));
-        attr = true;
-      }
-      grouped_tc_kernel<float, 3, GroupedProblem><<<p->grid, kGtThreads, GtCfg<3>::SMEM, s>>>(
-          p->table, p->count, p->total_tiles, p->counters, err);
-    }
-    return after_launch("grouped_tc");
+template <typename T, int P>
+static gbblas_status_t launch_grouped_tc(cudaStream_t s, gbblas_grouped_plan_s* p, int* err) {
+  if (p->n_ops > 0) {
+    grouped_split_kernel<T, P><<<dim3(unsigned(p->n_ops), 4), 256, 0, s>>>(p->ops);
+    GB_TRY(after_launch("grouped_split"));
   }
+  static bool attr = false;
+  if (!attr) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<P, GroupedProblem>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<P>::SMEM));
+    attr = true;
+  }
+  grouped_tc_kernel<P, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
+      p->table, p->tile_prob, p->maps, p->total_tiles, p->counters, err);
+  return after_launch("grouped_tc");
+}
+
+static gbblas_status_t launch_grouped(cudaStream_t s, gbblas_grouped_plan_s* p, int* err) {
+  if (p->method == 1)
+    return p->dtype == GBBLAS_DTYPE_BF16 ? launch_grouped_tc<__nv_bfloat16, 1>(s, p, err)
+                                         : launch_grouped_tc<float, 3>(s, p, err);
   if (p->dtype == GBBLAS_DTYPE_BF16)
     grouped_gemm_kernel<__nv_bfloat16><<<p->grid, kGThreads, 0, s>>>(p->table, p->count, p->total_tiles, p->counters);
   else
@@ -206,8 +218,7 @@ static int grouped_method() {
 extern "C" gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t plan) {
   if (!plan) return GBBLAS_STATUS_SUCCESS;
   if (plan->exec) cudaGraphExecDestroy(plan->exec);
-  if (plan->table) cudaFree(plan->table);
-  if (plan->counters) cudaFree(plan->counters);
+  if (plan->block) cudaFree(plan->block);
   delete plan;
   return GBBLAS_STATUS_SUCCESS;
 }
@@ -216,7 +227,8 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
                                    const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
                                    const void* const* a, const int64_t* lda, const void* const* b,
                                    const int64_t* ldb, const float* beta, float* const* c, const int64_t* ldc,
-                                   int tile_m, int tile_n, std::vector<GroupedProblem>& tab, int64_t& tiles) {
+                                   int tile_m, int tile_n, std::vector<GroupedProblem>& tab,
+                                   std::vector<int>& tile_prob, int64_t& tiles) {
   if (dtype != GBBLAS_DTYPE_F32 && dtype != GBBLAS_DTYPE_BF16)
     return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: element type must be F32 or BF16");
   if (count < 0 || count > (1 << 24)) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: bad problem count");
@@ -243,7 +255,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
     p.ta = ca != 'n';
     p.tb = cb != 'n';
     p.tiles_n = int(cdiv(n[i], tile_n));
-    p.tile_start = tiles;
+    p.tile_start = 0;
     p.alpha = alpha[i];
     p.beta = beta[i];
     p.a = a[i];
@@ -252,17 +264,217 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
     p.lda = lda[i];
     p.ldb = ldb[i];
     p.ldc = ldc[i];
-    tiles += cdiv(m[i], tile_m) * p.tiles_n;
     tab.push_back(p);
+  }
+  // longest tiles first; tiles numbered in that order
+  std::stable_sort(tab.begin(), tab.end(),
+                   [](const GroupedProblem& x, const GroupedProblem& y) { return x.k > y.k; });
+  tile_prob.clear();
+  for (size_t i = 0; i < tab.size(); ++i) {
+    GroupedProblem& p = tab[i];
+    p.tile_start = tiles;
+    const int64_t nt = cdiv(int64_t(p.m), tile_m) * p.tiles_n;
+    tiles += nt;
+    tile_prob.insert(tile_prob.end(), size_t(nt), int(i));
   }
   return GBBLAS_STATUS_SUCCESS;
 }
 
-static int grouped_grid(gbblas_handle_t h, int64_t tiles, int method, int dtype) {
-  // resident CTAs per SM: SIMT 8 x 256 threads; tcgen05 by shared memory
-  const int per_sm = method == 0 ? 8 : (dtype == GBBLAS_DTYPE_BF16 ? 2 : 1);
+// One operand of the tcgen05 path: converted into BF16 terms (offset into
+// the term area) or, for a BF16 operand already K-contiguous with a 16-byte
+// aligned leading dimension, mapped in place.
+struct TcOperandPlan {
+  int prob, which;  // which: 0 = A (rows m), 1 = B (rows n)
+  bool direct;
+  int64_t rows, k, sr, Kp;
+  const void* src;
+  size_t off;
+};
+
+static void plan_tc_operands(int dtype, const std::vector<GroupedProblem>& tab, std::vector<TcOperandPlan>& pl,
+                             size_t& term_bytes) {
+  const int P = dtype == GBBLAS_DTYPE_BF16 ? 1 : 3;
+  pl.clear();
+  term_bytes = 0;
+  for (size_t i = 0; i < tab.size(); ++i) {
+    const GroupedProblem& p = tab[i];
+    if (p.k == 0) continue;
+    for (int which = 0; which < 2; ++which) {
+      TcOperandPlan o{};
+      o.prob = int(i);
+      o.which = which;
+      o.k = p.k;
+      // A(m, k) = ta ? A[k + m*lda] : A[m + k*lda];  B as rows n: tb ? B[n + k*ldb] : B[k + n*ldb]
+      int64_t sk;
+      if (which == 0) {
+        o.rows = p.m;
+        o.sr = p.ta ? p.lda : 1;
+        sk = p.ta ? 1 : p.lda;
+        o.src = p.a;
+      } else {
+        o.rows = p.n;
+        o.sr = p.tb ? 1 : p.ldb;
+        sk = p.tb ? p.ldb : 1;
+        o.src = p.b;
+      }
+      o.direct = dtype == GBBLAS_DTYPE_BF16 && sk == 1 && o.sr % 8 == 0 && o.sr >= o.k &&
+                 (reinterpret_cast<uintptr_t>(o.src) & 15) == 0;
+      if (!o.direct) {
+        o.Kp = cdiv(o.k, int64_t(16)) * 16;
+        o.off = term_bytes;
+        term_bytes += (size_t(P) * size_t(o.rows) * size_t(o.Kp) * 2 + 255) & ~size_t(255);
+        o.sr = which == 0 ? (p.ta ? p.lda : 1) : (p.tb ? 1 : p.ldb);
+      }
+      pl.push_back(o);
+    }
+  }
+}
+
+// Tensor maps (two per problem) and the conversion list, once the term area
+// has its address.
+static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedProblem>& tab,
+                                          const std::vector<TcOperandPlan>& pl, uint8_t* terms,
+                                          std::vector<CUtensorMap>& maps, std::vector<GtOperand>& ops) {
+  EncodeTiledFn fn = tensor_map_encoder();
+  if (!fn) return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: cuTensorMapEncodeTiled unavailable");
+  const int P = dtype == GBBLAS_DTYPE_BF16 ? 1 : 3;
+  maps.assign(2 * std::max<size_t>(1, tab.size()), CUtensorMap{});
+  ops.clear();
+  for (const TcOperandPlan& o : pl) {
+    const GroupedProblem& p = tab[size_t(o.prob)];
+    void* base;
+    cuuint64_t dims[3], strides[2];
+    cuuint32_t box[3] = {cuuint32_t(kGtBK), cuuint32_t(o.which == 0 ? kGtBM : kGtBN), 1};
+    if (o.direct) {
+      base = const_cast<void*>(o.src);
+      dims[0] = cuuint64_t(o.k);
+      dims[1] = cuuint64_t(o.rows);
+      dims[2] = 1;
+      strides[0] = cuuint64_t(o.sr) * 2;
+      strides[1] = cuuint64_t(o.sr) * 2 * cuuint64_t(o.rows);
+    } else {
+      base = terms + o.off;
+      dims[0] = cuuint64_t(o.Kp);
+      dims[1] = cuuint64_t(o.rows);
+      dims[2] = cuuint64_t(P);
+      strides[0] = cuuint64_t(o.Kp) * 2;
+      strides[1] = cuuint64_t(o.Kp) * 2 * cuuint64_t(o.rows);
+      box[2] = cuuint32_t(P);
+      GtOperand g;
+      g.src = o.src;
+      g.sr = o.sr;
+      g.sk = o.which == 0 ? (p.ta ? 1 : p.lda) : (p.tb ? p.ldb : 1);
+      g.rows = int(o.rows);
+      g.K = int(o.k);
+      g.Kp = int(o.Kp);
+      g.blocks = int(gt_split_blocks(o.rows, o.Kp, g.sk == 1));
+      g.out = reinterpret_cast<__nv_bfloat16*>(terms + o.off);
+      ops.push_back(g);
+    }
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(&maps[size_t(2 * o.prob + o.which)], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides,
+                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+      return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: tensor map encode failed (" + std::to_string(int(r)) + ")");
+  }
+  // largest conversions first
+  std::stable_sort(ops.begin(), ops.end(), [](const GtOperand& x, const GtOperand& y) { return x.blocks > y.blocks; });
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+static size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Byte layout of a launch's device block.
+struct GroupedLayout {
+  size_t table, tile_prob, counters, maps, ops, terms, total;
+};
+
+static GroupedLayout grouped_layout(size_t count, size_t tiles, size_t n_maps, size_t n_ops, size_t term_bytes) {
+  GroupedLayout L;
+  L.table = 0;
+  L.tile_prob = round256(sizeof(GroupedProblem) * std::max<size_t>(1, count));
+  L.counters = L.tile_prob + round256(sizeof(int) * std::max<size_t>(1, tiles));
+  L.maps = L.counters + 256;
+  L.ops = L.maps + round256(sizeof(CUtensorMap) * n_maps);
+  L.terms = L.ops + round256(sizeof(GtOperand) * n_ops);
+  L.total = L.terms + term_bytes;
+  return L;
+}
+
+static int grouped_grid(gbblas_handle_t h, int64_t tiles, int method) {
+  // resident CTAs per SM: SIMT 8 x 256 threads; tcgen05 one (shared memory)
+  const int per_sm = method == 0 ? 8 : 1;
   const int64_t cap = int64_t(h->sm_count) * per_sm;
   return int(std::max<int64_t>(1, std::min<int64_t>(tiles, cap)));
+}
+
+// Builds everything a launch needs on the host, points `pl` into `block`
+// (which must hold layout.total bytes) and returns the host images to upload.
+struct GroupedHost {
+  std::vector<GroupedProblem> tab;
+  std::vector<int> tile_prob;
+  std::vector<TcOperandPlan> operands;
+  std::vector<CUtensorMap> maps;
+  std::vector<GtOperand> ops;
+  size_t term_bytes = 0;
+  int64_t tiles = 0;
+};
+
+static GroupedLayout bind_plan(gbblas_handle_t h, int dtype, int method, GroupedHost& H, void* block,
+                               gbblas_grouped_plan_s* pl) {
+  GroupedLayout L = grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.term_bytes);
+  uint8_t* b = static_cast<uint8_t*>(block);
+  pl->dtype = dtype;
+  pl->method = method;
+  pl->count = int(H.tab.size());
+  pl->total_tiles = H.tiles;
+  pl->grid = grouped_grid(h, H.tiles, method);
+  pl->table = reinterpret_cast<GroupedProblem*>(b + L.table);
+  pl->tile_prob = reinterpret_cast<int*>(b + L.tile_prob);
+  pl->counters = reinterpret_cast<unsigned long long*>(b + L.counters);
+  pl->maps = method == 1 ? reinterpret_cast<CUtensorMap*>(b + L.maps) : nullptr;
+  pl->ops = method == 1 ? reinterpret_cast<GtOperand*>(b + L.ops) : nullptr;
+  pl->n_ops = method == 1 ? int(H.ops.size()) : 0;
+  return L;
+}
+
+// Host-side preparation shared by plans and one-shot calls.  The term area's
+// address is only known once the block exists, so the maps are encoded
+// against `block` (may be null while sizing).
+static gbblas_status_t prepare_host(int dtype, int method, int64_t count, const char* transa, const char* transb,
+                                    const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
+                                    const void* const* a, const int64_t* lda, const void* const* b,
+                                    const int64_t* ldb, const float* beta, float* const* c, const int64_t* ldc,
+                                    GroupedHost& H) {
+  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                     method ? kGtBM : kGT, method ? kGtBN : kGT, H.tab, H.tile_prob, H.tiles));
+  if (method == 1) {
+    plan_tc_operands(dtype, H.tab, H.operands, H.term_bytes);
+    // sizes only: maps two per problem, one conversion per non-direct operand
+    H.maps.assign(2 * std::max<size_t>(1, H.tab.size()), CUtensorMap{});
+    size_t n_conv = 0;
+    for (const TcOperandPlan& o : H.operands) n_conv += o.direct ? 0 : 1;
+    H.ops.resize(n_conv);
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+static gbblas_status_t upload(const GroupedHost& H, const GroupedLayout& L, uint8_t* block, cudaStream_t s) {
+  if (!H.tab.empty())
+    GB_CUDA_TRY(cudaMemcpyAsync(block + L.table, H.tab.data(), sizeof(GroupedProblem) * H.tab.size(),
+                                cudaMemcpyHostToDevice, s));
+  if (!H.tile_prob.empty())
+    GB_CUDA_TRY(cudaMemcpyAsync(block + L.tile_prob, H.tile_prob.data(), sizeof(int) * H.tile_prob.size(),
+                                cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemsetAsync(block + L.counters, 0, 2 * sizeof(unsigned long long), s));
+  if (!H.maps.empty() && L.ops > L.maps)
+    GB_CUDA_TRY(cudaMemcpyAsync(block + L.maps, H.maps.data(), sizeof(CUtensorMap) * H.maps.size(),
+                                cudaMemcpyHostToDevice, s));
+  if (!H.ops.empty())
+    GB_CUDA_TRY(cudaMemcpyAsync(block + L.ops, H.ops.data(), sizeof(GtOperand) * H.ops.size(),
+                                cudaMemcpyHostToDevice, s));
+  return GBBLAS_STATUS_SUCCESS;
 }
 
 extern "C" {
@@ -277,28 +489,31 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
   if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "grouped: null handle");
   if (!out) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: null plan pointer");
   *out = nullptr;
-  std::vector<GroupedProblem> tab;
-  int64_t tiles = 0;
   const int method = grouped_method();
-  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
-                     method ? kGtBM : kGT, method ? kGtBN : kGT, tab, tiles));
+  GroupedHost H;
+  GB_TRY(prepare_host(dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
   auto* plan = new (std::nothrow) gbblas_grouped_plan_s();
   if (!plan) return fail(GBBLAS_STATUS_ALLOC_FAILED, "grouped: out of host memory");
-  plan->dtype = dtype;
-  plan->method = method;
   plan->err = h->dev_error;
-  plan->count = int(tab.size());
-  plan->total_tiles = tiles;
   plan->device = h->device;
-  plan->grid = grouped_grid(h, tiles, method, dtype);
-  cudaError_t e = cudaMalloc(&plan->table, sizeof(GroupedProblem) * std::max<size_t>(1, tab.size()));
-  if (e == cudaSuccess) e = cudaMalloc(&plan->counters, 2 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemset(plan->counters, 0, 2 * sizeof(unsigned long long));
-  if (e == cudaSuccess && !tab.empty())
-    e = cudaMemcpy(plan->table, tab.data(), sizeof(GroupedProblem) * tab.size(), cudaMemcpyHostToDevice);
+  const GroupedLayout L0 = grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.term_bytes);
+  cudaError_t e = cudaMalloc(&plan->block, L0.total);
   if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "grouped: plan allocation");
+  }
+  const GroupedLayout L = bind_plan(h, dtype, method, H, plan->block, plan);
+  gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
+  if (method == 1)
+    st = encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(plan->block) + L.terms, H.maps, H.ops);
+  if (st == GBBLAS_STATUS_SUCCESS) st = upload(H, L, static_cast<uint8_t*>(plan->block), h->stream);
+  if (st == GBBLAS_STATUS_SUCCESS) {
+    e = cudaStreamSynchronize(h->stream);  // the host images go out of scope
+    if (e != cudaSuccess) st = cuda_fail(e, "grouped: plan upload");
+  }
+  if (st != GBBLAS_STATUS_SUCCESS) {
     gbblas_grouped_plan_destroy(plan);
-    return cuda_fail(e, "grouped: plan upload");
+    return st;
   }
   *out = plan;
   return GBBLAS_STATUS_SUCCESS;
@@ -310,8 +525,8 @@ gbblas_status_t gbblas_grouped_plan_run(gbblas_handle_t h, gbblas_grouped_plan_t
   if (!plan) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: null plan");
   if (plan->total_tiles == 0) return GBBLAS_STATUS_SUCCESS;
   if (!plan->exec) {
-    // capture the persistent launch once on a private stream (the handle's
-    // stream may be the legacy default stream, which cannot be captured)
+    // capture the launch once on a private stream (the handle's stream may be
+    // the legacy default stream, which cannot be captured)
     cudaStream_t cs;
     GB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;
@@ -340,30 +555,21 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
                                     const int64_t* ldc) {
   clear_error();
   if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "grouped: null handle");
-  std::vector<GroupedProblem> tab;
-  int64_t tiles = 0;
   const int method = grouped_method();
-  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
-                     method ? kGtBM : kGT, method ? kGtBN : kGT, tab, tiles));
-  if (tiles == 0) return GBBLAS_STATUS_SUCCESS;
-  // one-shot: table and counters live in the handle's stream-ordered temp memory
-  const size_t tbytes = (sizeof(GroupedProblem) * tab.size() + 255) & ~size_t(255);
+  GroupedHost H;
+  GB_TRY(prepare_host(dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
+  if (H.tiles == 0) return GBBLAS_STATUS_SUCCESS;
+  // one-shot: the whole block lives in the handle's stream-ordered temp memory
+  const GroupedLayout L0 = grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.term_bytes);
   void* ws = nullptr;
-  GB_TRY(temp_acquire(h, tbytes + 256, &ws));
+  GB_TRY(temp_acquire(h, L0.total, &ws));
   gbblas_grouped_plan_s tmp;
-  tmp.dtype = dtype;
-  tmp.method = method;
-  tmp.count = int(tab.size());
-  tmp.total_tiles = tiles;
-  tmp.grid = grouped_grid(h, tiles, method, dtype);
-  tmp.table = static_cast<GroupedProblem*>(ws);
-  tmp.counters = reinterpret_cast<unsigned long long*>(static_cast<uint8_t*>(ws) + tbytes);
-  GB_CUDA_TRY(cudaMemcpyAsync(tmp.table, tab.data(), sizeof(GroupedProblem) * tab.size(), cudaMemcpyHostToDevice,
-                              h->stream));
-  GB_CUDA_TRY(cudaMemsetAsync(tmp.counters, 0, 2 * sizeof(unsigned long long), h->stream));
+  const GroupedLayout L = bind_plan(h, dtype, method, H, ws, &tmp);
+  if (method == 1)
+    GB_TRY(encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(ws) + L.terms, H.maps, H.ops));
+  GB_TRY(upload(H, L, static_cast<uint8_t*>(ws), h->stream));
   gbblas_status_t s = launch_grouped(h->stream, &tmp, h->dev_error);
-  tmp.table = nullptr;  // not owned
-  tmp.counters = nullptr;
+  // the host images (pageable) were staged by the copies before they returned
   return s;
 }
 

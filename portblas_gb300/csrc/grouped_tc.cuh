@@ -1,23 +1,40 @@
-// grouped_tc.cuh — tensor-core (tcgen05) tile kernel of the grouped GEMM.
+// grouped_tc.cuh — tensor-core (tcgen05) path of the grouped GEMM.
 //
-// Same scheduler as the SIMT grouped kernel (persistent CTAs, global atomic
-// tile counter, binary search over per-problem tile prefix sums), but each
-// 128 x 64 output tile runs on tcgen05.mma with a TMEM accumulator.  Grouped
-// problems have per-problem pointers, leading dimensions and transposes, so
-// operand tiles cannot come from one tensor map: the 128 threads of the CTA
-// gather them with ordinary loads (coalesced along whichever dimension is
-// contiguous), convert them to BF16 terms (FP32 inputs are split into three
-// terms, exact residuals, as in gemm_tc.cu) and store them in the same
-// 128-byte-swizzled K-major layout TMA would produce, so the MMA descriptors
-// are those of the TMA-fed kernel.  A proxy fence publishes the generic-proxy
-// stores to the tensor core before the stage's mbarrier arrival.
+// Two kernels, captured together in the plan's CUDA graph:
 //
-// Per k-block (64) and stage: P A-term tiles (128 x 64) and P B-term tiles
-// (64 x 64); two stages; 256 threads gather.  Thread 0 issues the MMAs (all
-// term pairs with a + b <= P - 1) and commits each stage back to the loaders.
-// Every 8 k-blocks the TMEM accumulator is promoted into FP32 registers (warp
-// w holds rows 32*(w%4).. and 32 of the 64 columns) so long K keeps
-// FP32-level accuracy.
+// 1. grouped_split_kernel<T, P>: converts every operand that needs it into
+//    K-major BF16 terms [P][rows][Kp] (Kp = k rounded up to 16, zero pad),
+//    any transpose absorbed through 32 x 32 shared-memory tiles so both the
+//    strided read and the K-contiguous write are coalesced.  FP32 inputs are
+//    split into P = 3 terms with exact residuals (as in gemm_tc.cu), so the
+//    six kept term products give FP32-level accuracy at any k; BF16 inputs
+//    are one term, and a BF16 operand that is already K-contiguous with a
+//    16-byte-aligned leading dimension is read in place (no conversion).
+//    Each element is converted once, however many output tiles read it.
+//
+// 2. grouped_tc_kernel<P>: persistent CTAs over the 128 x 64 output tiles of
+//    all problems (problems ordered by decreasing k, tiles numbered in that
+//    order, a global atomic counter hands them out).  Every operand has its
+//    own TMA tensor map (in device memory, two per problem), so the operand
+//    tiles stream in with cp.async.bulk.tensor exactly as in the dense
+//    kernel, and the pipeline never drains at a tile boundary:
+//      warp 6     scheduler: takes tile numbers from the counter, resolves
+//                 their problems and fills a ring of work slots ahead of the
+//                 other roles (and prefetches the tiles' tensor maps);
+//      warp 0     producer: issues the TMA loads of each slot's k-blocks into
+//                 an S-stage mbarrier ring (the P terms of A and of B in one
+//                 3-D box each);
+//      warp 1     allocates TMEM; one lane issues tcgen05.mma (M128 N64 K16)
+//                 for every term pair, commits each stage back to the
+//                 producer and each finished chunk of 8 k-blocks to one of
+//                 two TMEM accumulators;
+//      warps 2-5  epilogue: tcgen05.ld of each chunk into FP32 registers
+//                 (one output row of 64 columns per thread), then
+//                 alpha / beta and the stores to C, while the MMA warp is
+//                 already filling the other accumulator.
+// Every mbarrier wait is bounded: a wait that gives up records an error code
+// and its role stops; the others give up on their own bounded waits, the
+// producer waits for its copies in flight, and TMEM is freed.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -26,264 +43,416 @@
 
 namespace gb {
 
-constexpr int kGtBM = 128, kGtBN = 64, kGtBK = 64, kGtThreads = 256, kGtChunk = 8;
+constexpr int kGtBM = 128, kGtBN = 64, kGtBK = 64, kGtThreads = 224, kGtChunk = 8, kGtRing = 8;
 
 template <int P>
 struct GtCfg {
-  static constexpr int A_TILE = kGtBM * kGtBK * 2;  // 16 KB
-  static constexpr int B_TILE = kGtBN * kGtBK * 2;  //  8 KB
+  static constexpr int A_TILE = kGtBM * kGtBK * 2;  // 16 KB per term
+  static constexpr int B_TILE = kGtBN * kGtBK * 2;  //  8 KB per term
   static constexpr int STAGE = P * (A_TILE + B_TILE);
-  static constexpr int STAGES = 2;
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 128;
+  static constexpr int STAGES = P == 1 ? 8 : 3;
+  // barriers: full/empty per stage, two accumulator pairs, a work-slot pair per ring entry; then the TMEM address
+  static constexpr int BARRIER_BYTES = (2 * STAGES + 4 + 2 * kGtRing) * 8 + 4;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
   static constexpr int NPAIRS = P == 1 ? 1 : (P == 2 ? 3 : 6);
+  static constexpr int TMEM_COLS = 2 * kGtBN;  // two chunk accumulators
+  static_assert(BARRIER_BYTES <= 512, "barrier area");
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
+// One operand to convert: X(r, k) = src[r*sr + k*sk], r < rows, k < K,
+// written as out[p][r][k] for k < Kp (zeros for k >= K; Kp a multiple of 16
+// so every term row starts on a 32-byte sector).
+struct GtOperand {
+  const void* src;
+  int64_t sr, sk;
+  int rows, K, Kp, blocks;  // blocks: tiles of the mapping gt_split_blocks() picks
+  __nv_bfloat16* out;
+};
 
-// byte offset of 16-byte chunk c (k / 8) of row r in a 128 B-swizzled,
-// K-major tile (8-row groups 1024 B apart, chunk index XOR row % 8)
-__device__ __forceinline__ uint32_t sw128_offset(int r, int c) {
-  return uint32_t((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+// Tiles of an operand's conversion: K-contiguous operands (sk == 1) in
+// 32-row x 128-k tiles with no transpose, the others in 64 x 64 tiles
+// transposed through shared memory.
+__host__ __device__ inline int64_t gt_split_blocks(int64_t rows, int64_t Kp, bool kcontig) {
+  return kcontig ? ((rows + 31) / 32) * ((Kp + 127) / 128) : ((rows + 63) / 64) * ((Kp + 63) / 64);
 }
 
 template <typename T>
-__device__ __forceinline__ float ld_f32(const T* p);
+__device__ __forceinline__ float gt_ld(const T* p);
 template <>
-__device__ __forceinline__ float ld_f32<float>(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float gt_ld<float>(const float* p) { return __ldg(p); }
 template <>
-__device__ __forceinline__ float ld_f32<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
-
-__device__ __forceinline__ void load_vec8(const float* p, float* v) {
-  const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-}
-__device__ __forceinline__ void load_vec8(const __nv_bfloat16* p, float* v) {
-  const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
-  const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&a);
-#pragma unroll
-  for (int e = 0; e < 8; ++e) v[e] = __bfloat162float(h[e]);
+__device__ __forceinline__ float gt_ld<__nv_bfloat16>(const __nv_bfloat16* p) {
+  return __uint_as_float(uint32_t(__ldg(reinterpret_cast<const unsigned short*>(p))) << 16);
 }
 
-// Gathers NCH chunks of 8 consecutive k of one row (global row gr) of an
-// operand whose element (row, k) is at src[row*srow + k*sk]: load() issues
-// every global load of the k-block first (so they are all in flight
-// together), store() splits the values into P BF16 terms and writes one
-// 16-byte swizzled chunk per term.
-template <typename T, int NCH>
-struct RowGather {
-  float v[NCH][8];
-  __device__ __forceinline__ void load(const T* src, int64_t srow, int64_t sk, int64_t gr, int64_t rows, int64_t k0,
-                                       int64_t K, int c0) {
-    const bool row_ok = gr < rows;
-    const T* p = src + (row_ok ? gr : 0) * srow + (k0 + int64_t(c0) * 8) * sk;
-    const int64_t kleft = K - (k0 + int64_t(c0) * 8);  // valid k from the first chunk on
-    if (row_ok && kleft >= NCH * 8) {
-      if (sk == 1 && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
-        // K contiguous and 16-byte aligned: 128-bit loads
-#pragma unroll
-        for (int c = 0; c < NCH; ++c) load_vec8(p + c * 8, v[c]);
-      } else {
-        // interior: no per-element bounds checks, 32-bit strides
-        const int s = int(sk);
-#pragma unroll
-        for (int c = 0; c < NCH; ++c)
-#pragma unroll
-          for (int e = 0; e < 8; ++e) v[c][e] = ld_f32<T>(p + (c * 8 + e) * s);
-      }
+// Four consecutive values of one row at p (k .. k+3, those >= kend read as 0).
+template <typename T>
+__device__ __forceinline__ void gt_ld4(const T* p, int64_t k, int64_t kend, float (&v)[4]) {
+  if (k + 3 < kend) {
+    if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
       return;
     }
-#pragma unroll
-    for (int c = 0; c < NCH; ++c)
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int64_t kk = int64_t(c) * 8 + e;
-        v[c][e] = (row_ok && kk < kleft) ? ld_f32<T>(p + kk * sk) : 0.f;
-      }
-  }
-  template <int P>
-  __device__ __forceinline__ void store(uint8_t* tile0, int tile_bytes, int r, int c0) {
-#pragma unroll
-    for (int c = 0; c < NCH; ++c) {
-      const uint32_t off = sw128_offset(r, c0 + c);
-#pragma unroll
-      for (int p = 0; p < P; ++p) {
-        __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          h[e] = __float2bfloat16_rn(v[c][e]);
-          v[c][e] -= __bfloat162float(h[e]);  // exact residual for the next term
-        }
-        *reinterpret_cast<uint4*>(tile0 + p * tile_bytes + off) = *reinterpret_cast<const uint4*>(h);
-      }
+    if (sizeof(T) == 2 && (reinterpret_cast<uintptr_t>(p) & 7) == 0) {
+      const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+      v[0] = __uint_as_float(q.x << 16); v[1] = __uint_as_float(q.x & 0xffff0000u);
+      v[2] = __uint_as_float(q.y << 16); v[3] = __uint_as_float(q.y & 0xffff0000u);
+      return;
     }
   }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) v[e] = k + e < kend ? gt_ld<T>(p + e) : 0.f;
+}
+
+// P BF16 terms of n consecutive FP32 values, t_0 = bf16(x), t_{i+1} =
+// bf16(x - t_0 - ... - t_i) (exact residuals), packed two per word; term p of
+// pair e goes to w[p][e].
+template <int P, int NPAIR>
+__device__ __forceinline__ void gt_terms(float* x, uint32_t (&w)[P][NPAIR]) {
+#pragma unroll
+  for (int p = 0; p < P; ++p)
+#pragma unroll
+    for (int e = 0; e < NPAIR; ++e) {
+      const __nv_bfloat162 h2 = __floats2bfloat162_rn(x[2 * e], x[2 * e + 1]);
+      w[p][e] = *reinterpret_cast<const uint32_t*>(&h2);
+      if (p + 1 < P) {
+        x[2 * e] -= __uint_as_float(w[p][e] << 16);
+        x[2 * e + 1] -= __uint_as_float(w[p][e] & 0xffff0000u);
+      }
+    }
+}
+
+// CTA (o, y) converts tiles y, y + gridDim.y, ... of operand o.  Every
+// thread has 16 global loads in flight per tile and writes whole 32-byte
+// sectors of the term rows.
+template <typename T, int P>
+__global__ void __launch_bounds__(256) grouped_split_kernel(const GtOperand* __restrict__ ops) {
+  __shared__ float tile[64][65];  // transposing mapping: tile[k][r]
+  const GtOperand op = ops[blockIdx.x];
+  const T* __restrict__ X = static_cast<const T*>(op.src);
+  __nv_bfloat16* __restrict__ out = op.out;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int64_t plane = int64_t(op.rows) * op.Kp;
+  if (op.sk == 1) {
+    // K-contiguous: warp w converts rows 4w .. 4w+3 of the tile, lane l the
+    // four k from 4l (and from 4l + 128 ... in later tiles)
+    const int nkb = (op.Kp + 127) / 128;
+    for (int j = blockIdx.y; j < op.blocks; j += gridDim.y) {
+      const int64_t r0 = int64_t(j / nkb) * 32 + warp * 4, k = int64_t(j % nkb) * 128 + 4 * lane;
+      float v[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t r = r0 + i;
+        if (r < op.rows) {
+          gt_ld4<T>(X + r * op.sr + k, k, op.K, v[i]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) v[i][e] = 0.f;
+        }
+      }
+      if (k < op.Kp) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int64_t r = r0 + i;
+          if (r < op.rows) {
+            uint32_t w[P][2];
+            gt_terms<P, 2>(v[i], w);
+            __nv_bfloat16* o = out + r * op.Kp + k;
+#pragma unroll
+            for (int p = 0; p < P; ++p) *reinterpret_cast<uint2*>(o + p * plane) = make_uint2(w[p][0], w[p][1]);
+          }
+        }
+      }
+    }
+    return;
+  }
+  // rows contiguous (sr == 1): 64 x 64 tiles through shared memory; loads
+  // with lanes along r, then each thread writes 16-byte chunks (8 k) of two rows
+  const int nkb = (op.Kp + 63) / 64;
+  for (int j = blockIdx.y; j < op.blocks; j += gridDim.y) {
+    const int64_t r0 = int64_t(j / nkb) * 64, k0 = int64_t(j % nkb) * 64;
+    {
+      const int rr = t & 63;
+      const int64_t r = r0 + rr;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int kk = (t >> 6) + 4 * i;
+        const int64_t k = k0 + kk;
+        tile[kk][rr] = (r < op.rows && k < op.K) ? gt_ld<T>(X + r + k * op.sk) : 0.f;
+      }
+    }
+    __syncthreads();
+    const int c = t & 7;
+    const int64_t k = k0 + 8 * c;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rr = (t >> 3) + 32 * h;
+      const int64_t r = r0 + rr;
+      if (r < op.rows && k < op.Kp) {
+        float x[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = tile[8 * c + e][rr];
+        uint32_t w[P][4];
+        gt_terms<P, 4>(x, w);
+        __nv_bfloat16* o = out + r * op.Kp + k;
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+          *reinterpret_cast<uint4*>(o + p * plane) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One scheduled tile (prob < 0: no more tiles).
+struct GtWork {
+  int prob, nk, m0, n0;
 };
 
-enum : int { kErrGtFull = 401, kErrGtEmpty = 402, kErrGtAcc = 403 };
+enum : int { kErrGtProducer = 401, kErrGtMma = 402, kErrGtEpilogue = 403, kErrGtDrain = 404 };
 
-// probs / count / total_tiles / counters: as grouped_gemm_kernel (grouped.cu),
-// with tiles of 128 x 64.
-template <typename T, int P, class Prob>
-__global__ void __launch_bounds__(kGtThreads, 2)
-    grouped_tc_kernel(const Prob* __restrict__ probs, int count, int64_t total_tiles,
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
+
+// probs: problem table (tiles numbered in table order, row-major over each
+// problem's 128 x 64 tile grid); tile_prob[t]: problem of tile t; maps[2p],
+// maps[2p+1]: tensor maps of problem p's A terms ([P][m][Kp]) and B terms
+// ([P][n][Kp]), box 64 x rows x P; counters[0] = next tile, counters[1] =
+// CTAs finished (the last one resets both, so a graph can replay the launch).
+template <int P, class Prob>
+__global__ void __launch_bounds__(kGtThreads, 1)
+    grouped_tc_kernel(const Prob* __restrict__ probs, const int* __restrict__ tile_prob,
+                      const CUtensorMap* __restrict__ maps, int64_t total_tiles,
                       unsigned long long* __restrict__ counters, int* __restrict__ err) {
   using Cfg = GtCfg<P>;
+  constexpr int S = Cfg::STAGES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::STAGES * Cfg::STAGE);
-  uint64_t* empty = full + Cfg::STAGES;
-  uint64_t* accb = empty + Cfg::STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
-  __shared__ long long tile_sh;
-  __shared__ int prob_sh;
-  __shared__ int abort_sh;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * Cfg::STAGE);
+  uint64_t* empty = full + S;
+  uint64_t* tfull = empty + S;     // [2] chunk accumulator ready
+  uint64_t* tempty = tfull + 2;    // [2] chunk accumulator drained
+  uint64_t* wfull = tempty + 2;    // [kGtRing] work slot published
+  uint64_t* wempty = wfull + kGtRing;  // [kGtRing] work slot read by the producer, MMA warp and epilogue
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wempty + kGtRing);
+  __shared__ GtWork ring[kGtRing];
 
-  const int t = threadIdx.x, warp = t >> 5;
-  if (t == 0) {
-    for (int s = 0; s < Cfg::STAGES; ++s) {
-      tc::mbar_init(&full[s], kGtThreads);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(accb, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+    }
+    for (int r = 0; r < kGtRing; ++r) {
+      tc::mbar_init(&wfull[r], 1);
+      tc::mbar_init(&wempty[r], 6);  // producer + MMA warp + 4 epilogue warps
+    }
     tc::fence_mbar_init();
-    abort_sh = 0;
   }
-  if (warp == 0) {
-    tc::tmem_alloc(tmem_slot, kGtBN);
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, Cfg::TMEM_COLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  constexpr uint32_t idesc = tc::idesc_bf16_f32(kGtBM, kGtBN);
 
-  uint32_t it = 0;    // stage iterations so far (all threads agree)
-  uint32_t nacc = 0;  // accumulator commits so far
-  for (;;) {
-    if (t == 0) {
-      tile_sh = (long long)atomicAdd(&counters[0], 1ull);
-      if (tile_sh < total_tiles) {
-        int lo = 0, hi = count - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (probs[mid].tile_start <= tile_sh) lo = mid; else hi = mid - 1;
+  if (warp == 6) {
+    // ----------------------------------------------------------- scheduler --
+    if (lane == 0) {
+      for (uint32_t i = 0;; ++i) {
+        const int r = i % kGtRing;
+        if (!tc::mbar_wait(&wempty[r], ((i / kGtRing) & 1) ^ 1)) {
+          atomicExch(err, kErrGtProducer);
+          break;
         }
-        prob_sh = lo;
+        const long long tile = (long long)atomicAdd(&counters[0], 1ull);
+        GtWork w{-1, 0, 0, 0};
+        if (tile < total_tiles) {
+          const int p = __ldg(tile_prob + tile);
+          const Prob& pr = probs[p];
+          const int local = int(tile - pr.tile_start);
+          w.prob = p;
+          w.nk = pr.k > 0 ? (pr.k + kGtBK - 1) / kGtBK : 0;
+          w.m0 = (local / pr.tiles_n) * kGtBM;
+          w.n0 = (local % pr.tiles_n) * kGtBN;
+          if (w.nk > 0) {
+            tc::tma_prefetch_desc(maps + 2 * p);
+            tc::tma_prefetch_desc(maps + 2 * p + 1);
+          }
+        }
+        ring[r] = w;
+        tc::mbar_arrive(&wfull[r]);
+        if (w.prob < 0) break;
       }
     }
-    __syncthreads();
-    const long long tile = tile_sh;
-    if (tile >= total_tiles || abort_sh) break;
-    const Prob& pr = probs[prob_sh];
-    const int local = int(tile - pr.tile_start);
-    const int64_t m0 = int64_t(local / pr.tiles_n) * kGtBM, n0 = int64_t(local % pr.tiles_n) * kGtBN;
-    const T* A = static_cast<const T*>(pr.a);
-    const T* B = static_cast<const T*>(pr.b);
-    // A(m, k) = ta ? A[k + m*lda] : A[m + k*lda];  B as rows n: (tb ? B[n + k*ldb] : B[k + n*ldb])
-    const int64_t a_srow = pr.ta ? pr.lda : 1, a_sk = pr.ta ? 1 : pr.lda;
-    const int64_t b_srow = pr.tb ? 1 : pr.ldb, b_sk = pr.tb ? pr.ldb : 1;
-    const int nk = int((pr.k + kGtBK - 1) / kGtBK);
-    // warp w: TMEM lanes 32*(w%4) (rows), columns 32*(w/4) .. +31 of the tile
-    const int half = warp >> 2;
-    float sum[kGtBN / 2];
+  } else if (warp == 0) {
+    // ------------------------------------------------------------ producer --
+    if (lane == 0) {
+      uint32_t it = 0;
+      for (uint32_t i = 0;; ++i) {
+        const int r = i % kGtRing;
+        if (!tc::mbar_wait(&wfull[r], (i / kGtRing) & 1)) {
+          atomicExch(err, kErrGtProducer);
+          break;
+        }
+        const GtWork w = ring[r];
+        tc::mbar_arrive(&wempty[r]);
+        if (w.prob < 0) break;
+        if (w.nk == 0) continue;
+        const CUtensorMap* ma = maps + 2 * w.prob;
+        const CUtensorMap* mb = ma + 1;
+        tensormap_acquire(ma);
+        tensormap_acquire(mb);
+        bool ok = true;
+        for (int kb = 0; kb < w.nk; ++kb, ++it) {
+          const int s = it % S;
+          if (!tc::mbar_wait(&empty[s], ((it / S) & 1) ^ 1)) {
+            atomicExch(err, kErrGtProducer);
+            ok = false;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
+          uint8_t* st = smem + s * Cfg::STAGE;
+          tc::tma_load_3d(st, ma, &full[s], kb * kGtBK, w.m0, 0);
+          tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kb * kGtBK, w.n0, 0);
+        }
+        if (!ok) break;
+      }
+      // drain: every copy this thread issued has landed before the CTA exits
+      for (uint32_t j = it > uint32_t(S) ? it - S : 0u; j < it; ++j)
+        if (!tc::mbar_wait(&full[j % S], (j / S) & 1)) {
+          atomicExch(err, kErrGtDrain);
+          break;
+        }
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer --
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kGtBM, kGtBN);
+      uint32_t it = 0, g = 0;
+      bool ok = true;
+      for (uint32_t i = 0; ok; ++i) {
+        const int r = i % kGtRing;
+        if (!tc::mbar_wait(&wfull[r], (i / kGtRing) & 1)) {
+          atomicExch(err, kErrGtMma);
+          break;
+        }
+        const GtWork w = ring[r];
+        tc::mbar_arrive(&wempty[r]);
+        if (w.prob < 0) break;
+        const int nch = (w.nk + kGtChunk - 1) / kGtChunk;
+        for (int c = 0; c < nch && ok; ++c, ++g) {
+          const int b = g & 1;
+          if (!tc::mbar_wait(&tempty[b], ((g >> 1) & 1) ^ 1)) {
+            atomicExch(err, kErrGtMma);
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t acc = tmem + uint32_t(b * kGtBN);
+          const int kb1 = min(w.nk, (c + 1) * kGtChunk);
+          for (int kb = c * kGtChunk; kb < kb1; ++kb, ++it) {
+            const int s = it % S;
+            if (!tc::mbar_wait(&full[s], (it / S) & 1)) {
+              atomicExch(err, kErrGtMma);
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint8_t* st = smem + s * Cfg::STAGE;
 #pragma unroll
-    for (int i = 0; i < kGtBN / 2; ++i) sum[i] = 0.f;
-    RowGather<T, 4> ga;
-    RowGather<T, 2> gbt;
-    bool ok = true;
-    for (int kb = 0; kb < nk && ok; ++kb, ++it) {
-      const int s = it % Cfg::STAGES;
-      const uint32_t ph = (it / Cfg::STAGES) & 1;
-      uint8_t* st = smem + s * Cfg::STAGE;
-      const int64_t k0 = int64_t(kb) * kGtBK;
-      // A: 128 rows x 8 chunks, thread t takes row t%128, chunks 4*(t/128)..+3;
-      // B: 64 rows x 8 chunks, thread t takes row t%64, chunks 2*(t/64)..+1.
-      // The loads go out before the wait for the stage, overlapping the MMAs
-      // still reading it.
-      ga.load(A, a_srow, a_sk, m0 + (t & 127), pr.m, k0, pr.k, (t >> 7) * 4);
-      gbt.load(B, b_srow, b_sk, n0 + (t & 63), pr.n, k0, pr.k, (t >> 6) * 2);
-      if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
-        if (t == 0) atomicExch(err, kErrGtEmpty);
-        ok = false;
+            for (int q = 0; q < Cfg::NPAIRS; ++q) {
+              const int pa = (q == 2 || q == 4) ? 1 : (q == 5 ? 2 : 0);
+              const int pb = (q == 1 || q == 4) ? 1 : (q == 3 ? 2 : 0);
+              const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+              const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+#pragma unroll
+              for (int j = 0; j < kGtBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
+                tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, kb != c * kGtChunk || q != 0 || j != 0);
+            }
+            tc::mma_commit(&empty[s]);
+          }
+          if (ok) tc::mma_commit(&tfull[b]);
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue --
+    // warp w owns TMEM lanes [32*(w%4), +32): one output row per thread
+    const int q = warp & 3;
+    uint32_t g = 0;
+    for (uint32_t i = 0;; ++i) {
+      const int r = i % kGtRing;
+      if (!tc::mbar_wait(&wfull[r], (i / kGtRing) & 1)) {
+        if (lane == 0) atomicExch(err, kErrGtEpilogue);
         break;
       }
-      ga.template store<P>(st, Cfg::A_TILE, t & 127, (t >> 7) * 4);
-      gbt.template store<P>(st + P * Cfg::A_TILE, Cfg::B_TILE, t & 63, (t >> 6) * 2);
-      fence_proxy_async_smem();
-      tc::mbar_arrive(&full[s]);
-      const bool chunk_end = (kb + 1 == nk) || ((kb + 1) % kGtChunk == 0);
-      if (t == 0) {
-        if (!tc::mbar_wait(&full[s], ph)) {
-          atomicExch(err, kErrGtFull);
-          abort_sh = 1;
-        } else {
-          tc::tc_fence_after();
+      const GtWork w = ring[r];
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&wempty[r]);
+      if (w.prob < 0) break;
+      float sum[kGtBN];
 #pragma unroll
-          for (int q = 0; q < Cfg::NPAIRS; ++q) {
-            const int pa = (q == 2 || q == 4) ? 1 : (q == 5 ? 2 : 0);
-            const int pb = (q == 1 || q == 4) ? 1 : (q == 3 ? 2 : 0);
-            const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
-            const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
-#pragma unroll
-            for (int j = 0; j < kGtBK / 16; ++j)
-              tc::mma_bf16(tmem, ad + 2 * j, bd + 2 * j, idesc, (kb % kGtChunk) != 0 || q != 0 || j != 0);
-          }
-          tc::mma_commit(&empty[s]);
-          if (chunk_end) tc::mma_commit(accb);
-        }
-      }
-      if (chunk_end) {
-        // promote the chunk accumulator into registers
-        if (!tc::mbar_wait(accb, nacc & 1)) {
-          if (t == 0) atomicExch(err, kErrGtAcc);
+      for (int j = 0; j < kGtBN; ++j) sum[j] = 0.f;
+      const int nch = (w.nk + kGtChunk - 1) / kGtChunk;
+      bool ok = true;
+      for (int c = 0; c < nch; ++c, ++g) {
+        const int b = g & 1;
+        if (!tc::mbar_wait(&tfull[b], (g >> 1) & 1)) {
+          if (lane == 0) atomicExch(err, kErrGtEpilogue);
           ok = false;
+          break;
         }
-        ++nacc;
         tc::tc_fence_after();
-        if (ok) {
-          uint32_t r[32];
-          tc::tmem_ld_32x32b_x32(tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(half * 32), r);
+#pragma unroll
+        for (int c0 = 0; c0 < kGtBN; c0 += 32) {
+          uint32_t v[32];
+          tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kGtBN + c0), v);
           tc::tmem_ld_wait();
 #pragma unroll
-          for (int i = 0; i < 32; ++i) sum[i] += __uint_as_float(r[i]);
+          for (int j = 0; j < 32; ++j) sum[c0 + j] += __uint_as_float(v[j]);
         }
         tc::tc_fence_before();
-        __syncthreads();  // everyone has read TMEM before the next chunk's MMAs
-        if (abort_sh) ok = false;
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&tempty[b]);
       }
-    }
-    if (!ok) {
-      if (t == 0) abort_sh = 1;
-      __syncthreads();
-      break;
-    }
-    // epilogue: row m0 + 32*(warp%4) + lane, columns n0 + 32*half + i
-    const int64_t gm = m0 + (warp & 3) * 32 + (t & 31);
-    if (gm < pr.m) {
+      if (!ok) break;
+      const Prob& pr = probs[w.prob];
+      const int64_t gm = int64_t(w.m0) + q * 32 + lane;
+      if (gm < pr.m) {
+        float* const c = pr.c;
+        const int64_t ldc = pr.ldc;
+        const float alpha = pr.alpha, beta = pr.beta;
+        const int nleft = pr.n - w.n0;
 #pragma unroll
-      for (int i = 0; i < kGtBN / 2; ++i) {
-        const int64_t gn = n0 + half * 32 + i;
-        if (gn < pr.n) {
-          float* cp = pr.c + gm + gn * pr.ldc;
-          float v = pr.alpha * sum[i];
-          if (pr.beta != 0.f) v = fmaf(pr.beta, *cp, v);
-          *cp = v;
+        for (int j = 0; j < kGtBN; ++j) {
+          if (j < nleft) {
+            float* cp = c + gm + (int64_t(w.n0) + j) * ldc;
+            float v = alpha * sum[j];
+            if (beta != 0.f) v = fmaf(beta, *cp, v);
+            *cp = v;
+          }
         }
       }
     }
-    __syncthreads();
   }
-  // let the last MMAs and copies settle, free TMEM, reset the scheduler
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, kGtBN);
+    tc::tmem_dealloc(tmem, Cfg::TMEM_COLS);
   }
-  if (t == 0) {
+  if (threadIdx.x == 0) {
     __threadfence();
     const unsigned long long done = atomicAdd(&counters[1], 1ull);
     if (done == gridDim.x - 1) {
