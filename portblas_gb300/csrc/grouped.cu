@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kGThreads) grouped_gemm_kernel(const GroupedPr
 // CUDA graph of the launch.
 struct gbblas_grouped_plan_s {
   int dtype = 0;
-  int method = 1;  // 1: tcgen05 tiles (128 x 64), 0: SIMT tiles (64 x 64)
+  int method = 1;  // 1: tcgen05 tiles (128 x 128), 0: SIMT tiles (64 x 64)
   int count = 0;
   int64_t total_tiles = 0;
   int grid = 0;

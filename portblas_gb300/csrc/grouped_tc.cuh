@@ -12,24 +12,24 @@
 //    16-byte-aligned leading dimension is read in place (no conversion).
 //    Each element is converted once, however many output tiles read it.
 //
-// 2. grouped_tc_kernel<P>: persistent CTAs over the 128 x 64 output tiles of
+// 2. grouped_tc_kernel<P>: persistent CTAs over the 128 x 128 output tiles of
 //    all problems (problems ordered by decreasing k, tiles numbered in that
 //    order, a global atomic counter hands them out).  Every operand has its
 //    own TMA tensor map (in device memory, two per problem), so the operand
 //    tiles stream in with cp.async.bulk.tensor exactly as in the dense
 //    kernel, and the pipeline never drains at a tile boundary:
-//      warp 6     scheduler: takes tile numbers from the counter, resolves
+//      warp 2     scheduler: takes tile numbers from the counter, resolves
 //                 their problems and fills a ring of work slots ahead of the
 //                 other roles (and prefetches the tiles' tensor maps);
 //      warp 0     producer: issues the TMA loads of each slot's k-blocks into
 //                 an S-stage mbarrier ring (the P terms of A and of B in one
 //                 3-D box each);
-//      warp 1     allocates TMEM; one lane issues tcgen05.mma (M128 N64 K16)
+//      warp 1     allocates TMEM; one lane issues tcgen05.mma (M128 N128 K16)
 //                 for every term pair, commits each stage back to the
 //                 producer and each finished chunk of 8 k-blocks to one of
 //                 two TMEM accumulators;
-//      warps 2-5  epilogue: tcgen05.ld of each chunk into FP32 registers
-//                 (one output row of 64 columns per thread), then
+//      warps 3-10 epilogue: tcgen05.ld of each chunk into FP32 registers
+//                 (64 columns of one output row per thread), then
 //                 alpha / beta and the stores to C, while the MMA warp is
 //                 already filling the other accumulator.
 // Every mbarrier wait is bounded: a wait that gives up records an error code
@@ -43,19 +43,23 @@
 
 namespace gb {
 
-constexpr int kGtBM = 128, kGtBN = 64, kGtBK = 64, kGtThreads = 224, kGtChunk = 8, kGtRing = 8;
+// Warps: 0 producer, 1 MMA issuer, 2 scheduler, 3..10 epilogue.
+constexpr int kGtBM = 128, kGtBN = 128, kGtBK = 64, kGtEpiWarps = 8, kGtThreads = 32 * (3 + kGtEpiWarps),
+              kGtChunk = 8, kGtRing = 8;
+// TMEM chunk accumulators (the MMA warp runs up to kGtAcc - 1 chunks ahead of the epilogue)
+constexpr int kGtAcc = 2;
 
 template <int P>
 struct GtCfg {
   static constexpr int A_TILE = kGtBM * kGtBK * 2;  // 16 KB per term
   static constexpr int B_TILE = kGtBN * kGtBK * 2;  //  8 KB per term
   static constexpr int STAGE = P * (A_TILE + B_TILE);
-  static constexpr int STAGES = P == 1 ? 8 : 3;
+  static constexpr int STAGES = P == 1 ? 6 : 2;
   // barriers: full/empty per stage, two accumulator pairs, a work-slot pair per ring entry; then the TMEM address
-  static constexpr int BARRIER_BYTES = (2 * STAGES + 4 + 2 * kGtRing) * 8 + 4;
+  static constexpr int BARRIER_BYTES = (2 * STAGES + 2 * kGtAcc + 2 * kGtRing) * 8 + 4;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
   static constexpr int NPAIRS = P == 1 ? 1 : (P == 2 ? 3 : 6);
-  static constexpr int TMEM_COLS = 2 * kGtBN;  // two chunk accumulators
+  static constexpr int TMEM_COLS = kGtAcc * kGtBN;  // the chunk accumulators
   static_assert(BARRIER_BYTES <= 512, "barrier area");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
@@ -128,7 +132,7 @@ __device__ __forceinline__ void gt_terms(float* x, uint32_t (&w)[P][NPAIR]) {
 // thread has 16 global loads in flight per tile and writes whole 32-byte
 // sectors of the term rows.
 template <typename T, int P>
-__global__ void __launch_bounds__(256) grouped_split_kernel(const GtOperand* __restrict__ ops) {
+__global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* __restrict__ ops) {
   __shared__ float tile[64][65];  // transposing mapping: tile[k][r]
   const GtOperand op = ops[blockIdx.x];
   const T* __restrict__ X = static_cast<const T*>(op.src);
@@ -208,18 +212,25 @@ __global__ void __launch_bounds__(256) grouped_split_kernel(const GtOperand* __r
 
 // One scheduled tile (prob < 0: no more tiles).
 struct GtWork {
-  int prob, nk, m0, n0;
+  int prob, nk, m0, n0;  // problem, k-blocks, tile origin
+  int m, n;              // the problem's C extent
+  float alpha, beta;
+  float* c;
+  int64_t ldc;
 };
+
+// tiles the scheduler takes from the counter at a time
+constexpr int kGtBatch = 8;
 
 enum : int { kErrGtProducer = 401, kErrGtMma = 402, kErrGtEpilogue = 403, kErrGtDrain = 404 };
 
 __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
-  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
                : "memory");
 }
 
 // probs: problem table (tiles numbered in table order, row-major over each
-// problem's 128 x 64 tile grid); tile_prob[t]: problem of tile t; maps[2p],
+// problem's 128 x 128 tile grid); tile_prob[t]: problem of tile t; maps[2p],
 // maps[2p+1]: tensor maps of problem p's A terms ([P][m][Kp]) and B terms
 // ([P][n][Kp]), box 64 x rows x P; counters[0] = next tile, counters[1] =
 // CTAs finished (the last one resets both, so a graph can replay the launch).
@@ -234,9 +245,9 @@ __global__ void __launch_bounds__(kGtThreads, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * Cfg::STAGE);
   uint64_t* empty = full + S;
-  uint64_t* tfull = empty + S;     // [2] chunk accumulator ready
-  uint64_t* tempty = tfull + 2;    // [2] chunk accumulator drained
-  uint64_t* wfull = tempty + 2;    // [kGtRing] work slot published
+  uint64_t* tfull = empty + S;         // [kGtAcc] chunk accumulator ready
+  uint64_t* tempty = tfull + kGtAcc;   // [kGtAcc] chunk accumulator drained
+  uint64_t* wfull = tempty + kGtAcc;   // [kGtRing] work slot published
   uint64_t* wempty = wfull + kGtRing;  // [kGtRing] work slot read by the producer, MMA warp and epilogue
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wempty + kGtRing);
   __shared__ GtWork ring[kGtRing];
@@ -247,13 +258,13 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kGtAcc; ++b) {
       tc::mbar_init(&tfull[b], 1);
-      tc::mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+      tc::mbar_init(&tempty[b], kGtEpiWarps);  // one arrival per epilogue warp
     }
     for (int r = 0; r < kGtRing; ++r) {
       tc::mbar_init(&wfull[r], 1);
-      tc::mbar_init(&wempty[r], 6);  // producer + MMA warp + 4 epilogue warps
+      tc::mbar_init(&wempty[r], 2 + kGtEpiWarps);  // producer + MMA warp + epilogue warps
     }
     tc::fence_mbar_init();
   }
@@ -266,17 +277,20 @@ __global__ void __launch_bounds__(kGtThreads, 1)
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 6) {
+  if (warp == 2) {
     // ----------------------------------------------------------- scheduler --
-    if (lane == 0) {
-      for (uint32_t i = 0;; ++i) {
-        const int r = i % kGtRing;
-        if (!tc::mbar_wait(&wempty[r], ((i / kGtRing) & 1) ^ 1)) {
-          atomicExch(err, kErrGtProducer);
-          break;
-        }
-        const long long tile = (long long)atomicAdd(&counters[0], 1ull);
-        GtWork w{-1, 0, 0, 0};
+    // kGtBatch tiles per atomic; their lookups run in parallel on the lanes
+    __shared__ GtWork batch[kGtBatch];
+    uint32_t i = 0;
+    bool more = true;
+    while (more) {
+      long long base = 0;
+      if (lane == 0) base = (long long)atomicAdd(&counters[0], (unsigned long long)kGtBatch);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (lane < kGtBatch) {
+        const long long tile = base + lane;
+        GtWork w{};
+        w.prob = -1;
         if (tile < total_tiles) {
           const int p = __ldg(tile_prob + tile);
           const Prob& pr = probs[p];
@@ -285,20 +299,44 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           w.nk = pr.k > 0 ? (pr.k + kGtBK - 1) / kGtBK : 0;
           w.m0 = (local / pr.tiles_n) * kGtBM;
           w.n0 = (local % pr.tiles_n) * kGtBN;
+          w.m = pr.m;
+          w.n = pr.n;
+          w.alpha = pr.alpha;
+          w.beta = pr.beta;
+          w.c = pr.c;
+          w.ldc = pr.ldc;
           if (w.nk > 0) {
             tc::tma_prefetch_desc(maps + 2 * p);
             tc::tma_prefetch_desc(maps + 2 * p + 1);
           }
         }
-        ring[r] = w;
-        tc::mbar_arrive(&wfull[r]);
-        if (w.prob < 0) break;
+        batch[lane] = w;
       }
+      __syncwarp();
+      if (lane == 0) {
+        for (int l = 0; l < kGtBatch; ++l, ++i) {
+          const int r = i % kGtRing;
+          if (!tc::mbar_wait(&wempty[r], ((i / kGtRing) & 1) ^ 1)) {
+            atomicExch(err, kErrGtProducer);
+            more = false;
+            break;
+          }
+          ring[r] = batch[l];
+          tc::mbar_arrive(&wfull[r]);
+          if (batch[l].prob < 0) {
+            more = false;
+            break;
+          }
+        }
+      }
+      more = __shfl_sync(0xffffffffu, more, 0);
+      __syncwarp();
     }
   } else if (warp == 0) {
     // ------------------------------------------------------------ producer --
     if (lane == 0) {
       uint32_t it = 0;
+      int fenced = -1;  // problem whose tensor maps this thread last fenced
       for (uint32_t i = 0;; ++i) {
         const int r = i % kGtRing;
         if (!tc::mbar_wait(&wfull[r], (i / kGtRing) & 1)) {
@@ -311,8 +349,11 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         if (w.nk == 0) continue;
         const CUtensorMap* ma = maps + 2 * w.prob;
         const CUtensorMap* mb = ma + 1;
-        tensormap_acquire(ma);
-        tensormap_acquire(mb);
+        if (w.prob != fenced) {  // once per run of tiles of one problem
+          tensormap_acquire(ma);
+          tensormap_acquire(mb);
+          fenced = w.prob;
+        }
         bool ok = true;
         for (int kb = 0; kb < w.nk; ++kb, ++it) {
           const int s = it % S;
@@ -352,8 +393,8 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         if (w.prob < 0) break;
         const int nch = (w.nk + kGtChunk - 1) / kGtChunk;
         for (int c = 0; c < nch && ok; ++c, ++g) {
-          const int b = g & 1;
-          if (!tc::mbar_wait(&tempty[b], ((g >> 1) & 1) ^ 1)) {
+          const int b = g % kGtAcc;
+          if (!tc::mbar_wait(&tempty[b], ((g / kGtAcc) & 1) ^ 1)) {
             atomicExch(err, kErrGtMma);
             ok = false;
             break;
@@ -388,8 +429,9 @@ __global__ void __launch_bounds__(kGtThreads, 1)
     }
   } else {
     // ------------------------------------------------------------ epilogue --
-    // warp w owns TMEM lanes [32*(w%4), +32): one output row per thread
-    const int q = warp & 3;
+    // warp w owns TMEM lanes [32*(w%4), +32) (one output row per thread) and
+    // columns [64*h, +64), h = (w - 3) / 4
+    const int q = warp & 3, h = (warp - 3) >> 2;
     uint32_t g = 0;
     for (uint32_t i = 0;; ++i) {
       const int r = i % kGtRing;
@@ -401,23 +443,23 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&wempty[r]);
       if (w.prob < 0) break;
-      float sum[kGtBN];
+      float sum[64];
 #pragma unroll
-      for (int j = 0; j < kGtBN; ++j) sum[j] = 0.f;
+      for (int j = 0; j < 64; ++j) sum[j] = 0.f;
       const int nch = (w.nk + kGtChunk - 1) / kGtChunk;
       bool ok = true;
       for (int c = 0; c < nch; ++c, ++g) {
-        const int b = g & 1;
-        if (!tc::mbar_wait(&tfull[b], (g >> 1) & 1)) {
+        const int b = g % kGtAcc;
+        if (!tc::mbar_wait(&tfull[b], (g / kGtAcc) & 1)) {
           if (lane == 0) atomicExch(err, kErrGtEpilogue);
           ok = false;
           break;
         }
         tc::tc_fence_after();
 #pragma unroll
-        for (int c0 = 0; c0 < kGtBN; c0 += 32) {
+        for (int c0 = 0; c0 < 64; c0 += 32) {
           uint32_t v[32];
-          tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kGtBN + c0), v);
+          tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kGtBN + h * 64 + c0), v);
           tc::tmem_ld_wait();
 #pragma unroll
           for (int j = 0; j < 32; ++j) sum[c0 + j] += __uint_as_float(v[j]);
@@ -427,17 +469,16 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         if (lane == 0) tc::mbar_arrive(&tempty[b]);
       }
       if (!ok) break;
-      const Prob& pr = probs[w.prob];
       const int64_t gm = int64_t(w.m0) + q * 32 + lane;
-      if (gm < pr.m) {
-        float* const c = pr.c;
-        const int64_t ldc = pr.ldc;
-        const float alpha = pr.alpha, beta = pr.beta;
-        const int nleft = pr.n - w.n0;
+      if (gm < w.m) {
+        float* const c = w.c;
+        const int64_t ldc = w.ldc;
+        const float alpha = w.alpha, beta = w.beta;
+        const int nleft = w.n - w.n0 - h * 64;
+        float* cp = c + gm + (int64_t(w.n0) + h * 64) * ldc;
 #pragma unroll
-        for (int j = 0; j < kGtBN; ++j) {
+        for (int j = 0; j < 64; ++j, cp += ldc) {
           if (j < nleft) {
-            float* cp = c + gm + (int64_t(w.n0) + j) * ldc;
             float v = alpha * sum[j];
             if (beta != 0.f) v = fmaf(beta, *cp, v);
             *cp = v;
