@@ -37,44 +37,77 @@ gbblas_status_t launch_gemm_simt(gbblas_handle_t h, const GemmArgs<double>& g) {
 
 // ------------------------------------------------------ small batches --
 // Strided batches of small problems (M, N, K <= 64): one CTA per problem
-// loads all of A and B into shared memory in one coalesced pass (a single
-// wait instead of one per k-slab), each of 256 threads computes a 4x4 block,
-// and C goes back through shared memory so the stores are coalesced too.
+// loads all of A and B into shared memory in one coalesced pass (128-bit
+// loads along the contiguous dimension when it is 16-byte aligned), each of
+// 256 threads computes a 4x4 block from 128-bit shared reads, and C goes
+// back through shared memory so the stores are coalesced too.
 constexpr int kSmallMax = 64;
 
+// S[k][r] <- X(r, k) for r < R, k < K, X(r, k) = X[r*sr + k*sk] with one of
+// sr, sk equal to 1 (RC: rows contiguous).  Thread t takes vector t % 16 of
+// the contiguous dimension and strides the other by 16.
+template <bool RC>
+__device__ __forceinline__ void small_stage(float (&S)[kSmallMax][kSmallMax + 4], const float* __restrict__ X,
+                                            int64_t ld, int R, int K, int t) {
+  const int v = t & 15, o = t >> 4;
+  const int C = RC ? R : K;  // contiguous extent
+  const int O = RC ? K : R;  // other extent
+  const bool vec = (C & 3) == 0 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  if (vec) {
+    if (4 * v < C)
+      for (int q = o; q < O; q += 16) {
+        const float4 x = __ldg(reinterpret_cast<const float4*>(X + int64_t(q) * ld) + v);
+        if (RC) {  // rows contiguous: S[q][4v..4v+3]
+          *reinterpret_cast<float4*>(&S[q][4 * v]) = x;
+        } else {  // k contiguous: S[4v..4v+3][q]
+          S[4 * v][q] = x.x;
+          S[4 * v + 1][q] = x.y;
+          S[4 * v + 2][q] = x.z;
+          S[4 * v + 3][q] = x.w;
+        }
+      }
+    return;
+  }
+  for (int q = o; q < O; q += 16)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int c = 4 * v + e;
+      if (c < C) {
+        const float x = __ldg(X + int64_t(q) * ld + c);
+        if (RC) S[q][c] = x;
+        else S[c][q] = x;
+      }
+    }
+}
+
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) gemm_small_batched_kernel(GemmArgs<float> g) {
-  __shared__ float As[kSmallMax][kSmallMax + 4];  // [k][i]
-  __shared__ float Bs[kSmallMax][kSmallMax + 4];  // [k][j]
+__global__ void __launch_bounds__(256, 6) gemm_small_batched_kernel(GemmArgs<float> g) {
+  __shared__ __align__(16) float As[kSmallMax][kSmallMax + 4];  // [k][i]
+  __shared__ __align__(16) float Bs[kSmallMax][kSmallMax + 4];  // [k][j]
   const int64_t bz = blockIdx.x;
   const float* A = g.a + bz * g.stride_a;
   const float* B = g.b + bz * g.stride_b;
   float* C = g.c + bz * g.stride_c;
   const int M = int(g.m), N = int(g.n), K = int(g.k), t = threadIdx.x;
-  for (int e = t; e < M * K; e += 256) {
-    int i, k;
-    if (!TA) { i = e % M; k = e / M; } else { k = e % K; i = e / K; }
-    As[k][i] = TA ? A[k + int64_t(i) * g.lda] : A[i + int64_t(k) * g.lda];
-  }
-  for (int e = t; e < K * N; e += 256) {
-    int k, j;
-    if (!TB) { k = e % K; j = e / K; } else { j = e % N; k = e / N; }
-    Bs[k][j] = TB ? B[j + int64_t(k) * g.ldb] : B[k + int64_t(j) * g.ldb];
-  }
+  // A(i, k) = TA ? A[k + i*lda] : A[i + k*lda];  B(k, j) = TB ? B[j + k*ldb] : B[k + j*ldb]
+  small_stage<!TA>(As, A, g.lda, M, K, t);
+  small_stage<TB>(Bs, B, g.ldb, N, K, t);
   __syncthreads();
   const int tx = t % 16, ty = t / 16;
   float acc[4][4] = {};
   for (int k = 0; k < K; ++k) {
-    float a[4], b[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      a[q] = As[k][ty * 4 + q];
-      b[q] = Bs[k][tx * 4 + q];
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    const float4 a = *reinterpret_cast<const float4*>(&As[k][ty * 4]);
+    const float4 b = *reinterpret_cast<const float4*>(&Bs[k][tx * 4]);
+#define GB_ROW(i, ai)                         \
+  acc[i][0] = fmaf(ai, b.x, acc[i][0]);       \
+  acc[i][1] = fmaf(ai, b.y, acc[i][1]);       \
+  acc[i][2] = fmaf(ai, b.z, acc[i][2]);       \
+  acc[i][3] = fmaf(ai, b.w, acc[i][3]);
+    GB_ROW(0, a.x)
+    GB_ROW(1, a.y)
+    GB_ROW(2, a.z)
+    GB_ROW(3, a.w)
+#undef GB_ROW
   }
   __syncthreads();
   // stage C in As as [j][i] for coalesced column-major stores
@@ -83,13 +116,14 @@ __global__ void __launch_bounds__(256) gemm_small_batched_kernel(GemmArgs<float>
 #pragma unroll
     for (int j = 0; j < 4; ++j) As[tx * 4 + j][ty * 4 + i] = acc[i][j];
   __syncthreads();
-  for (int e = t; e < M * N; e += 256) {
-    const int i = e % M, j = e / M;
-    float* cp = C + i + int64_t(j) * g.ldc;
-    float v = g.alpha * As[j][i];
-    if (g.beta != 0.f) v = fmaf(g.beta, *cp, v);
-    *cp = v;
-  }
+  const int i = t & 63;
+  if (i < M)
+    for (int j = t >> 6; j < N; j += 4) {
+      float* cp = C + i + int64_t(j) * g.ldc;
+      float v = g.alpha * As[j][i];
+      if (g.beta != 0.f) v = fmaf(g.beta, *cp, v);
+      *cp = v;
+    }
 }
 
 bool small_batched_applies(const GemmArgs<float>& g, int sm_count) {

@@ -290,3 +290,53 @@ def test_gemm_strided_small_batch_path(sb, torch_cuda, ta, tb, m, n, k, beta):
         np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * k)
         np.testing.assert_array_equal(out[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:],
                                       c[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:])
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("m,n,k", [(64, 64, 64), (32, 48, 16), (8, 4, 12)])
+def test_gemm_strided_small_batch_vector_loads(sb, torch_cuda, ta, tb, m, n, k):
+    """Small-batch kernel with 16-byte-aligned operands (the 128-bit load
+    path): exact leading dimensions and strides that are multiples of 4."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    g = rng(7 * m + n + k)
+    batch = 640
+    lda, ldb, ldc = (k if ta else m), (n if tb else k), m
+    sa, sbs, sc = lda * (m if ta else k), ldb * (k if tb else n), ldc * n
+    a = g.uniform(-1, 1, sa * batch).astype(np.float32)
+    b = g.uniform(-1, 1, sbs * batch).astype(np.float32)
+    c = g.uniform(-1, 1, sc * batch).astype(np.float32)
+    cd = to_dev(c, torch)
+    blas._gemm_strided_batched(sb, "t" if ta else "n", "t" if tb else "n", m, n, k, 1.0, to_dev(a, torch), lda, sa,
+                               to_dev(b, torch), ldb, sbs, 0.5, cd, ldc, sc, batch)
+    out = to_host(cd)
+    for i in (0, 3, 333, batch - 1):
+        ref = oracle.gemm(ta, tb, m, n, k, 1.0, a[i * sa:], lda, b[i * sbs:], ldb, 0.5, c[i * sc:], ldc)
+        got = out[i * sc:(i + 1) * sc].reshape(n, ldc).T
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * k)
+
+
+@pytest.mark.parametrize("mode", ["auto", "fp32_simt", "split_bf16x6"])
+def test_gemm_tall_skinny_split_k(sb, torch_cuda, mode):
+    """Tall-skinny reduction-dimension shapes (M = N = 48, K = 2^18) take the
+    split-K partial + reduction path; sampled entries against the FP64 oracle
+    within the FP32 accumulation bound."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(getattr(blas.sgemm_mode_t, mode))
+    g = rng(99)
+    m = n = 48
+    k = 1 << 18
+    a = g.uniform(-1, 1, m * k).astype(np.float32)
+    b = g.uniform(-1, 1, k * n).astype(np.float32)
+    cd = torch.zeros(m * n, device="cuda")
+    blas._gemm(sb, "n", "n", m, n, k, 1.0, to_dev(a, torch), m, to_dev(b, torch), k, 0.0, cd, m)
+    got = to_host(cd).reshape(n, m).T
+    rows = g.integers(0, m, 24)
+    cols = g.integers(0, n, 24)
+    ref = oracle.gemm(False, False, m, n, k, 1.0, a, m, b, k, 0.0, None, m, rows=rows, cols=cols)
+    scale = oracle.gemm_absscale(False, False, m, n, k, 1.0, a, m, b, k, 0.0, None, m, rows=rows, cols=cols)
+    err = np.abs(got[rows, cols] - ref) / scale
+    assert err.max() <= 2.0 * (k + 4) * 2.0 ** -24, err.max()
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
