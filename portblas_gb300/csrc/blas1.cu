@@ -299,8 +299,20 @@ __device__ __forceinline__ typename Op::Acc block_reduce(typename Op::Acc a, typ
 
 // VEC: x (and y) contiguous and 16-byte aligned; otherwise strided scalar
 // loads from the view base (negative increments allowed).
+// Resident CTAs per SM the kernel is compiled for (and the grid is sized
+// to): 4 x 512 threads (32 registers) for FP32, 2 for FP64; nrm2's three
+// accumulators need more than 32 registers, so 3.
+template <class Op, typename T>
+struct Blas1Occupancy {
+  static constexpr int kCtas = sizeof(T) == 4 ? 4 : 2;
+};
+template <>
+struct Blas1Occupancy<Nrm2Op<float>, float> {
+  static constexpr int kCtas = 3;
+};
+
 template <class Op, typename T, bool VEC, bool HAS_Y>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) blas1_reduce(int64_t n, const T* __restrict__ x, int64_t incx,
+__global__ void __launch_bounds__(kThreads, Blas1Occupancy<Op, T>::kCtas) blas1_reduce(int64_t n, const T* __restrict__ x, int64_t incx,
                                                          const T* __restrict__ y, int64_t incy,
                                                          typename Op::Acc* __restrict__ partials,
                                                          unsigned int* __restrict__ ticket,
@@ -381,7 +393,7 @@ gbblas_status_t launch_reduce(gbblas_handle_t h, int64_t n, const T* x, int64_t 
   const bool vec = incx == 1 && aligned16(x) && (!HAS_Y || (incy == 1 && aligned16(y)));
   const int64_t per_block = int64_t(kThreads) * (vec ? 16 / int(sizeof(T)) : 1) * kUnroll;
   int64_t blocks = cdiv(n > 0 ? n : 1, per_block);
-  const int64_t cap = int64_t(h->sm_count) * (2048 / kThreads) * 1;
+  const int64_t cap = int64_t(h->sm_count) * Blas1Occupancy<Op, T>::kCtas;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   void* tmp = nullptr;

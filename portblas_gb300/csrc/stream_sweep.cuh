@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(kStThreads)
   uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
   uint64_t* empty = full + kStStages;
   T* xs = reinterpret_cast<T*>(empty + kStStages);  // [rows_per_split] when HAS_X
-  __shared__ bool is_last;
+  __shared__ unsigned long long last_mask;  // bit c: this CTA folds column tile ct0 + c
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ct0 = int64_t(blockIdx.x) * ctiles;          // first column tile of this CTA
@@ -291,24 +291,27 @@ __global__ void __launch_bounds__(kStThreads)
   }
   if (gridDim.y == 1) return;
   __threadfence();
+  if (threadIdx.x == 0) last_mask = 0ull;
   __syncthreads();
-  // last CTA (over the row chunks) of each column tile folds its 16 columns
-  for (int c = 0; c < nct; ++c) {
-    const int64_t ct = ct0 + c;
-    if (threadIdx.x == 0) is_last = atomicAdd(tickets + ct, 1u) == gridDim.y - 1;
-    __syncthreads();
-    if (is_last) {
-      __threadfence();
-      const int64_t col = ct * BC + threadIdx.x;
-      if (threadIdx.x < BC && col < N) {
-        Acc f = ldcg_any(partials + col);
-        for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + col));
-        pol.finish(f, col);
-      }
-      if (threadIdx.x == 0) tickets[ct] = 0u;
+  // the last CTA (over the row chunks) of each column tile folds its 16
+  // columns; the tickets of all this CTA's tiles are taken at once (thread c
+  // takes tile c), so the tail costs one round trip, not one per tile
+  if (threadIdx.x < nct && atomicAdd(tickets + ct0 + threadIdx.x, 1u) == gridDim.y - 1)
+    atomicOr(&last_mask, 1ull << threadIdx.x);
+  __syncthreads();
+  const unsigned long long mine = last_mask;
+  if (mine == 0ull) return;
+  __threadfence();
+  for (int idx = threadIdx.x; idx < nct * BC; idx += blockDim.x) {
+    const int c = idx / BC;
+    const int64_t col = (ct0 + c) * BC + idx % BC;
+    if (((mine >> c) & 1ull) && col < N) {
+      Acc f = ldcg_any(partials + col);
+      for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + col));
+      pol.finish(f, col);
     }
-    __syncthreads();
   }
+  if (threadIdx.x < nct && ((mine >> threadIdx.x) & 1ull)) tickets[ct0 + threadIdx.x] = 0u;
 }
 
 // ------------------------------------------------------------------ host --
