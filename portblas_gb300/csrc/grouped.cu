@@ -189,11 +189,11 @@ static gbblas_status_t launch_grouped_tc(cudaStream_t s, gbblas_grouped_plan_s* 
   }
   static bool attr = false;
   if (!attr) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<P, GroupedProblem>,
+    GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<P, kGtChunk, GroupedProblem>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<P>::SMEM));
     attr = true;
   }
-  grouped_tc_kernel<P, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
+  grouped_tc_kernel<P, kGtChunk, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
       p->table, p->tile_prob, p->maps, p->total_tiles, p->counters, err);
   return after_launch("grouped_tc");
 }

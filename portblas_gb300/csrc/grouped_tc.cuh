@@ -26,7 +26,7 @@
 //                 3-D box each);
 //      warp 1     allocates TMEM; one lane issues tcgen05.mma (M128 N128 K16)
 //                 for every term pair, commits each stage back to the
-//                 producer and each finished chunk of 8 k-blocks to one of
+//                 producer and each finished chunk of CHUNK k-blocks to one of
 //                 two TMEM accumulators;
 //      warps 3-10 epilogue: tcgen05.ld of each chunk into FP32 registers
 //                 (64 columns of one output row per thread), then
@@ -45,7 +45,7 @@ namespace gb {
 
 // Warps: 0 producer, 1 MMA issuer, 2 scheduler, 3..10 epilogue.
 constexpr int kGtBM = 128, kGtBN = 128, kGtBK = 64, kGtEpiWarps = 8, kGtThreads = 32 * (3 + kGtEpiWarps),
-              kGtChunk = 8, kGtRing = 8;
+              kGtChunk = 8, kGtRing = 8, kGtGroupM = 8;
 // TMEM chunk accumulators (the MMA warp runs up to kGtAcc - 1 chunks ahead of the epilogue)
 constexpr int kGtAcc = 2;
 
@@ -54,7 +54,7 @@ struct GtCfg {
   static constexpr int A_TILE = kGtBM * kGtBK * 2;  // 16 KB per term
   static constexpr int B_TILE = kGtBN * kGtBK * 2;  //  8 KB per term
   static constexpr int STAGE = P * (A_TILE + B_TILE);
-  static constexpr int STAGES = P == 1 ? 6 : 2;
+  static constexpr int STAGES = P == 1 ? 6 : (P == 2 ? 3 : 2);
   // barriers: full/empty per stage, two accumulator pairs, a work-slot pair per ring entry; then the TMEM address
   static constexpr int BARRIER_BYTES = (2 * STAGES + 2 * kGtAcc + 2 * kGtRing) * 8 + 4;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
@@ -229,12 +229,12 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
                : "memory");
 }
 
-// probs: problem table (tiles numbered in table order, row-major over each
-// problem's 128 x 128 tile grid); tile_prob[t]: problem of tile t; maps[2p],
-// maps[2p+1]: tensor maps of problem p's A terms ([P][m][Kp]) and B terms
+// probs: problem table (tiles numbered in table order; within a problem
+// down groups of kGtGroupM tile rows, then along N); tile_prob[t]: problem
+// of tile t; maps[2p], maps[2p+1]: tensor maps of problem p's A terms ([P][m][Kp]) and B terms
 // ([P][n][Kp]), box 64 x rows x P; counters[0] = next tile, counters[1] =
 // CTAs finished (the last one resets both, so a graph can replay the launch).
-template <int P, class Prob>
+template <int P, int CHUNK, class Prob>
 __global__ void __launch_bounds__(kGtThreads, 1)
     grouped_tc_kernel(const Prob* __restrict__ probs, const int* __restrict__ tile_prob,
                       const CUtensorMap* __restrict__ maps, int64_t total_tiles,
@@ -297,8 +297,14 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           const int local = int(tile - pr.tile_start);
           w.prob = p;
           w.nk = pr.k > 0 ? (pr.k + kGtBK - 1) / kGtBK : 0;
-          w.m0 = (local / pr.tiles_n) * kGtBM;
-          w.n0 = (local % pr.tiles_n) * kGtBN;
+          // tiles of a problem go down kGtGroupM M tiles, then along N, so the
+          // CTAs working at the same time share A and B panels in L2
+          const int tiles_m = (pr.m + kGtBM - 1) / kGtBM;
+          const int per_group = kGtGroupM * pr.tiles_n;
+          const int first_m = (local / per_group) * kGtGroupM, in = local % per_group;
+          const int gsize = min(tiles_m - first_m, kGtGroupM);
+          w.m0 = (first_m + in % gsize) * kGtBM;
+          w.n0 = (in / gsize) * kGtBN;
           w.m = pr.m;
           w.n = pr.n;
           w.alpha = pr.alpha;
@@ -391,7 +397,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         const GtWork w = ring[r];
         tc::mbar_arrive(&wempty[r]);
         if (w.prob < 0) break;
-        const int nch = (w.nk + kGtChunk - 1) / kGtChunk;
+        const int nch = (w.nk + CHUNK - 1) / CHUNK;
         for (int c = 0; c < nch && ok; ++c, ++g) {
           const int b = g % kGtAcc;
           if (!tc::mbar_wait(&tempty[b], ((g / kGtAcc) & 1) ^ 1)) {
@@ -401,8 +407,8 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           }
           tc::tc_fence_after();
           const uint32_t acc = tmem + uint32_t(b * kGtBN);
-          const int kb1 = min(w.nk, (c + 1) * kGtChunk);
-          for (int kb = c * kGtChunk; kb < kb1; ++kb, ++it) {
+          const int kb1 = min(w.nk, (c + 1) * CHUNK);
+          for (int kb = c * CHUNK; kb < kb1; ++kb, ++it) {
             const int s = it % S;
             if (!tc::mbar_wait(&full[s], (it / S) & 1)) {
               atomicExch(err, kErrGtMma);
@@ -419,7 +425,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
               const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
 #pragma unroll
               for (int j = 0; j < kGtBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
-                tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, kb != c * kGtChunk || q != 0 || j != 0);
+                tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, kb != c * CHUNK || q != 0 || j != 0);
             }
             tc::mma_commit(&empty[s]);
           }
@@ -446,7 +452,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       float sum[64];
 #pragma unroll
       for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-      const int nch = (w.nk + kGtChunk - 1) / kGtChunk;
+      const int nch = (w.nk + CHUNK - 1) / CHUNK;
       bool ok = true;
       for (int c = 0; c < nch; ++c, ++g) {
         const int b = g % kGtAcc;
