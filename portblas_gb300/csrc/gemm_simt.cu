@@ -126,12 +126,164 @@ __global__ void __launch_bounds__(256, 6) gemm_small_batched_kernel(GemmArgs<flo
     }
 }
 
+// ------------------------------------------- small batches, pipelined --
+// The 16-byte-aligned case (M, N, K multiples of 4, leading dimensions and
+// strides multiples of 4 floats): persistent CTAs walk the batch and copy
+// problem p+1's A and B into the second of two shared buffers with
+// cp.async while they compute problem p, so loads and FMAs overlap inside
+// every CTA.  Operands keep their memory layout in shared memory (64 rows of
+// 64 floats; rows whose k is contiguous have their 16-byte chunks XOR-
+// swizzled by row / 4 so the per-thread 128-bit reads hit distinct banks);
+// the inner loop takes 4 k at a time as 4 + 4 128-bit reads for 64 FMAs.
+constexpr int kPipeRow = 64;                         // floats per shared row
+constexpr int kPipeTile = kSmallMax * kPipeRow;      // floats per operand buffer
+constexpr int kPipeCtasPerSm = 3;                    // 64 KB of buffers each
+
+__device__ __forceinline__ int pipe_swz(int row, int chunk) { return (chunk ^ ((row >> 2) & 7)) * 4; }
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// rows x cols floats of X (row r at X + r*ld, cols contiguous) into S;
+// SWZ: chunk c of row r goes to chunk c ^ ((r / 4) % 8)
+template <bool SWZ>
+__device__ __forceinline__ void pipe_copy(float* S, const float* X, int64_t ld, int rows, int cols, int t) {
+  const int cpr = cols >> 2;  // chunks per row
+  for (int e = t; e < rows * 16; e += 256) {
+    const int r = e >> 4, c = e & 15;
+    if (c < cpr) cp_async16(S + r * kPipeRow + (SWZ ? pipe_swz(r, c) : 4 * c), X + int64_t(r) * ld + 4 * c);
+  }
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256, kPipeCtasPerSm) gemm_small_batched_pipe_kernel(GemmArgs<float> g) {
+  extern __shared__ __align__(16) float pipe_smem[];  // [2][A, B][kPipeTile]
+  const int M = int(g.m), N = int(g.n), K = int(g.k), t = threadIdx.x;
+  const int tx = t % 16, ty = t / 16;
+  // A(i, k): TA ? rows i, k contiguous (swizzled) : rows k, i contiguous
+  // B(k, j): TB ? rows k, j contiguous : rows j, k contiguous (swizzled)
+  auto issue = [&](int64_t p, int buf) {
+    float* SA = pipe_smem + buf * 2 * kPipeTile;
+    float* SB = SA + kPipeTile;
+    const float* A = g.a + p * g.stride_a;
+    const float* B = g.b + p * g.stride_b;
+    if (TA) pipe_copy<true>(SA, A, g.lda, M, K, t);
+    else pipe_copy<false>(SA, A, g.lda, K, M, t);
+    if (TB) pipe_copy<false>(SB, B, g.ldb, K, N, t);
+    else pipe_copy<true>(SB, B, g.ldb, N, K, t);
+    cp_async_commit();
+  };
+  int64_t p = blockIdx.x;
+  if (p < g.batch) issue(p, 0);
+  for (int buf = 0; p < g.batch; p += gridDim.x, buf ^= 1) {
+    const int64_t pn = p + gridDim.x;
+    if (pn < g.batch) {
+      issue(pn, buf ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const float* SA = pipe_smem + buf * 2 * kPipeTile;
+    const float* SB = SA + kPipeTile;
+    float acc[4][4] = {};
+    // swizzled operands: this thread's rows 4ty.. / 4tx.. share one XOR key
+    const float* ra = SA + (TA ? 4 * ty * kPipeRow : 4 * ty);
+    const float* rb = SB + (TB ? 4 * tx : 4 * tx * kPipeRow);
+    const int ka = ty & 7, kb = tx & 7;
+#pragma unroll 4
+    for (int k = 0; k < K; k += 4) {
+      float a[4][4], b[4][4];  // a[i][kk], b[kk][j]
+      const int oa = TA ? ((k >> 2) ^ ka) * 4 : k * kPipeRow;
+      const int ob = TB ? k * kPipeRow : ((k >> 2) ^ kb) * 4;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (TA) {  // row 4ty+q, k..k+3
+          const float4 v = *reinterpret_cast<const float4*>(ra + q * kPipeRow + oa);
+          a[q][0] = v.x; a[q][1] = v.y; a[q][2] = v.z; a[q][3] = v.w;
+        } else {  // row k+q, i = 4ty..4ty+3
+          const float4 v = *reinterpret_cast<const float4*>(ra + q * kPipeRow + oa);
+          a[0][q] = v.x; a[1][q] = v.y; a[2][q] = v.z; a[3][q] = v.w;
+        }
+        if (TB) {  // row k+q, j = 4tx..4tx+3
+          const float4 v = *reinterpret_cast<const float4*>(rb + q * kPipeRow + ob);
+          b[q][0] = v.x; b[q][1] = v.y; b[q][2] = v.z; b[q][3] = v.w;
+        } else {  // row 4tx+q (column j), k..k+3
+          const float4 v = *reinterpret_cast<const float4*>(rb + q * kPipeRow + ob);
+          b[0][q] = v.x; b[1][q] = v.y; b[2][q] = v.z; b[3][q] = v.w;
+        }
+      }
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i][kk], b[kk][j], acc[i][j]);
+    }
+    // C(i, j) for i = 4ty.., j = 4tx..: each column's 4 rows as one 128-bit access
+    float* C = g.c + p * g.stride_c;
+    if (4 * ty < M) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int gj = 4 * tx + j;
+        if (gj < N) {
+          float4* cp = reinterpret_cast<float4*>(C + 4 * ty + int64_t(gj) * g.ldc);
+          float4 v = make_float4(g.alpha * acc[0][j], g.alpha * acc[1][j], g.alpha * acc[2][j], g.alpha * acc[3][j]);
+          if (g.beta != 0.f) {
+            const float4 o = *cp;
+            v.x = fmaf(g.beta, o.x, v.x);
+            v.y = fmaf(g.beta, o.y, v.y);
+            v.z = fmaf(g.beta, o.z, v.z);
+            v.w = fmaf(g.beta, o.w, v.w);
+          }
+          *cp = v;
+        }
+      }
+    }
+    __syncthreads();  // this buffer is refilled by the next iteration's prefetch
+  }
+}
+
+static bool small_pipe_applies(const GemmArgs<float>& g) {
+  auto a16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+  return g.m % 4 == 0 && g.n % 4 == 0 && g.k % 4 == 0 && g.k > 0 && g.lda % 4 == 0 && g.ldb % 4 == 0 &&
+         g.ldc % 4 == 0 && g.stride_a % 4 == 0 && g.stride_b % 4 == 0 && g.stride_c % 4 == 0 && a16(g.a) &&
+         a16(g.b) && a16(g.c) && g.alpha != 0.f;
+}
+
 bool small_batched_applies(const GemmArgs<float>& g, int sm_count) {
   return g.m <= kSmallMax && g.n <= kSmallMax && g.k <= kSmallMax && g.batch >= 4 * int64_t(sm_count) &&
          g.batch <= INT32_MAX;
 }
 
 gbblas_status_t launch_gemm_small_batched(gbblas_handle_t h, const GemmArgs<float>& g) {
+  if (small_pipe_applies(g)) {
+    constexpr int smem = 4 * kPipeTile * int(sizeof(float));
+    const int64_t cap = int64_t(h->sm_count) * kPipeCtasPerSm;
+    const unsigned grid = unsigned(g.batch < cap ? g.batch : cap);
+#define GB_PIPE(TA_, TB_)                                                                                    \
+  if (g.ta == TA_ && g.tb == TB_) {                                                                          \
+    static bool attr = false;                                                                                \
+    if (!attr) {                                                                                             \
+      GB_CUDA_TRY(cudaFuncSetAttribute(gemm_small_batched_pipe_kernel<TA_, TB_>,                             \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));                  \
+      attr = true;                                                                                           \
+    }                                                                                                        \
+    gemm_small_batched_pipe_kernel<TA_, TB_><<<grid, 256, smem, h->stream>>>(g);                             \
+  }
+    GB_PIPE(false, false)
+    GB_PIPE(false, true)
+    GB_PIPE(true, false)
+    GB_PIPE(true, true)
+#undef GB_PIPE
+    return after_launch("gemm_small_batched_pipe");
+  }
   const dim3 grid(unsigned(g.batch));
 #define GB_SMALL(TA_, TB_) \
   if (g.ta == TA_ && g.tb == TB_) gemm_small_batched_kernel<TA_, TB_><<<grid, 256, 0, h->stream>>>(g);
