@@ -174,6 +174,8 @@ struct gbblas_grouped_plan_s {
   CUtensorMap* maps = nullptr;
   gb::GtOperand* ops = nullptr;
   int n_ops = 0;
+  int2* ctas = nullptr;  // (operand, part) of each split-pass CTA
+  int n_ctas = 0;
   cudaGraphExec_t exec = nullptr;
   int device = 0;
   int* err = nullptr;  // device error word of the creating handle
@@ -184,7 +186,7 @@ using namespace gb;
 template <typename T, int P>
 static gbblas_status_t launch_grouped_tc(cudaStream_t s, gbblas_grouped_plan_s* p, int* err) {
   if (p->n_ops > 0) {
-    grouped_split_kernel<T, P><<<dim3(unsigned(p->n_ops), 4), 256, 0, s>>>(p->ops);
+    grouped_split_kernel<T, P><<<unsigned(p->n_ctas), 256, 0, s>>>(p->ops, p->ctas);
     GB_TRY(after_launch("grouped_split"));
   }
   static bool attr = false;
@@ -289,6 +291,7 @@ struct TcOperandPlan {
   int64_t rows, k, sr, Kp;
   const void* src;
   size_t off;
+  int64_t sk;
 };
 
 static void plan_tc_operands(int dtype, const std::vector<GroupedProblem>& tab, std::vector<TcOperandPlan>& pl,
@@ -317,6 +320,7 @@ static void plan_tc_operands(int dtype, const std::vector<GroupedProblem>& tab, 
         sk = p.tb ? p.ldb : 1;
         o.src = p.b;
       }
+      o.sk = sk;
       o.direct = dtype == GBBLAS_DTYPE_BF16 && sk == 1 && o.sr % 8 == 0 && o.sr >= o.k &&
                  (reinterpret_cast<uintptr_t>(o.src) & 15) == 0;
       if (!o.direct) {
@@ -334,7 +338,8 @@ static void plan_tc_operands(int dtype, const std::vector<GroupedProblem>& tab, 
 // has its address.
 static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedProblem>& tab,
                                           const std::vector<TcOperandPlan>& pl, uint8_t* terms,
-                                          std::vector<CUtensorMap>& maps, std::vector<GtOperand>& ops) {
+                                          std::vector<CUtensorMap>& maps, std::vector<GtOperand>& ops,
+                                          std::vector<int2>& ctas) {
   EncodeTiledFn fn = tensor_map_encoder();
   if (!fn) return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: cuTensorMapEncodeTiled unavailable");
   const int P = dtype == GBBLAS_DTYPE_BF16 ? 1 : 3;
@@ -368,6 +373,7 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
       g.K = int(o.k);
       g.Kp = int(o.Kp);
       g.blocks = int(gt_split_blocks(o.rows, o.Kp, g.sk == 1));
+      g.parts = int(cdiv(int64_t(g.blocks), int64_t(kGtSplitTiles)));
       g.out = reinterpret_cast<__nv_bfloat16*>(terms + o.off);
       ops.push_back(g);
     }
@@ -380,6 +386,9 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
   }
   // largest conversions first
   std::stable_sort(ops.begin(), ops.end(), [](const GtOperand& x, const GtOperand& y) { return x.blocks > y.blocks; });
+  ctas.clear();
+  for (size_t i = 0; i < ops.size(); ++i)
+    for (int part = 0; part < ops[i].parts; ++part) ctas.push_back(make_int2(int(i), part));
   return GBBLAS_STATUS_SUCCESS;
 }
 
@@ -387,17 +396,19 @@ static size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte layout of a launch's device block.
 struct GroupedLayout {
-  size_t table, tile_prob, counters, maps, ops, terms, total;
+  size_t table, tile_prob, counters, maps, ops, ctas, terms, total;
 };
 
-static GroupedLayout grouped_layout(size_t count, size_t tiles, size_t n_maps, size_t n_ops, size_t term_bytes) {
+static GroupedLayout grouped_layout(size_t count, size_t tiles, size_t n_maps, size_t n_ops, size_t n_ctas,
+                                    size_t term_bytes) {
   GroupedLayout L;
   L.table = 0;
   L.tile_prob = round256(sizeof(GroupedProblem) * std::max<size_t>(1, count));
   L.counters = L.tile_prob + round256(sizeof(int) * std::max<size_t>(1, tiles));
   L.maps = L.counters + 256;
   L.ops = L.maps + round256(sizeof(CUtensorMap) * n_maps);
-  L.terms = L.ops + round256(sizeof(GtOperand) * n_ops);
+  L.ctas = L.ops + round256(sizeof(GtOperand) * n_ops);
+  L.terms = L.ctas + round256(sizeof(int2) * n_ctas);
   L.total = L.terms + term_bytes;
   return L;
 }
@@ -417,13 +428,15 @@ struct GroupedHost {
   std::vector<TcOperandPlan> operands;
   std::vector<CUtensorMap> maps;
   std::vector<GtOperand> ops;
+  std::vector<int2> ctas;
   size_t term_bytes = 0;
   int64_t tiles = 0;
 };
 
 static GroupedLayout bind_plan(gbblas_handle_t h, int dtype, int method, GroupedHost& H, void* block,
                                gbblas_grouped_plan_s* pl) {
-  GroupedLayout L = grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.term_bytes);
+  GroupedLayout L =
+      grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(), H.term_bytes);
   uint8_t* b = static_cast<uint8_t*>(block);
   pl->dtype = dtype;
   pl->method = method;
@@ -436,6 +449,8 @@ static GroupedLayout bind_plan(gbblas_handle_t h, int dtype, int method, Grouped
   pl->maps = method == 1 ? reinterpret_cast<CUtensorMap*>(b + L.maps) : nullptr;
   pl->ops = method == 1 ? reinterpret_cast<GtOperand*>(b + L.ops) : nullptr;
   pl->n_ops = method == 1 ? int(H.ops.size()) : 0;
+  pl->ctas = method == 1 ? reinterpret_cast<int2*>(b + L.ctas) : nullptr;
+  pl->n_ctas = method == 1 ? int(H.ctas.size()) : 0;
   return L;
 }
 
@@ -453,9 +468,14 @@ static gbblas_status_t prepare_host(int dtype, int method, int64_t count, const 
     plan_tc_operands(dtype, H.tab, H.operands, H.term_bytes);
     // sizes only: maps two per problem, one conversion per non-direct operand
     H.maps.assign(2 * std::max<size_t>(1, H.tab.size()), CUtensorMap{});
-    size_t n_conv = 0;
-    for (const TcOperandPlan& o : H.operands) n_conv += o.direct ? 0 : 1;
+    size_t n_conv = 0, n_ctas = 0;
+    for (const TcOperandPlan& o : H.operands)
+      if (!o.direct) {
+        ++n_conv;
+        n_ctas += size_t(cdiv(gt_split_blocks(o.rows, o.Kp, o.sk == 1), int64_t(kGtSplitTiles)));
+      }
     H.ops.resize(n_conv);
+    H.ctas.resize(n_ctas);
   }
   return GBBLAS_STATUS_SUCCESS;
 }
@@ -473,6 +493,9 @@ static gbblas_status_t upload(const GroupedHost& H, const GroupedLayout& L, uint
                                 cudaMemcpyHostToDevice, s));
   if (!H.ops.empty())
     GB_CUDA_TRY(cudaMemcpyAsync(block + L.ops, H.ops.data(), sizeof(GtOperand) * H.ops.size(),
+                                cudaMemcpyHostToDevice, s));
+  if (!H.ctas.empty())
+    GB_CUDA_TRY(cudaMemcpyAsync(block + L.ctas, H.ctas.data(), sizeof(int2) * H.ctas.size(),
                                 cudaMemcpyHostToDevice, s));
   return GBBLAS_STATUS_SUCCESS;
 }
@@ -496,7 +519,8 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
   if (!plan) return fail(GBBLAS_STATUS_ALLOC_FAILED, "grouped: out of host memory");
   plan->err = h->dev_error;
   plan->device = h->device;
-  const GroupedLayout L0 = grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.term_bytes);
+  const GroupedLayout L0 =
+      grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(), H.term_bytes);
   cudaError_t e = cudaMalloc(&plan->block, L0.total);
   if (e != cudaSuccess) {
     delete plan;
@@ -505,7 +529,8 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
   const GroupedLayout L = bind_plan(h, dtype, method, H, plan->block, plan);
   gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
   if (method == 1)
-    st = encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(plan->block) + L.terms, H.maps, H.ops);
+    st = encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(plan->block) + L.terms, H.maps, H.ops,
+                            H.ctas);
   if (st == GBBLAS_STATUS_SUCCESS) st = upload(H, L, static_cast<uint8_t*>(plan->block), h->stream);
   if (st == GBBLAS_STATUS_SUCCESS) {
     e = cudaStreamSynchronize(h->stream);  // the host images go out of scope
@@ -560,13 +585,14 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
   GB_TRY(prepare_host(dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
   if (H.tiles == 0) return GBBLAS_STATUS_SUCCESS;
   // one-shot: the whole block lives in the handle's stream-ordered temp memory
-  const GroupedLayout L0 = grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.term_bytes);
+  const GroupedLayout L0 =
+      grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(), H.term_bytes);
   void* ws = nullptr;
   GB_TRY(temp_acquire(h, L0.total, &ws));
   gbblas_grouped_plan_s tmp;
   const GroupedLayout L = bind_plan(h, dtype, method, H, ws, &tmp);
   if (method == 1)
-    GB_TRY(encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(ws) + L.terms, H.maps, H.ops));
+    GB_TRY(encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(ws) + L.terms, H.maps, H.ops, H.ctas));
   GB_TRY(upload(H, L, static_cast<uint8_t*>(ws), h->stream));
   gbblas_status_t s = launch_grouped(h->stream, &tmp, h->dev_error);
   // the host images (pageable) were staged by the copies before they returned

@@ -71,8 +71,13 @@ struct GtOperand {
   const void* src;
   int64_t sr, sk;
   int rows, K, Kp, blocks;  // blocks: tiles of the mapping gt_split_blocks() picks
+  int parts;                // CTAs sharing the operand's tiles
   __nv_bfloat16* out;
 };
+
+// tiles each CTA of the split pass converts (an operand of b tiles gets
+// ceil(b / kGtSplitTiles) CTAs, so every CTA has about the same work)
+constexpr int kGtSplitTiles = 2;
 
 // Tiles of an operand's conversion: K-contiguous operands (sk == 1) in
 // 32-row x 128-k tiles with no transpose, the others in 64 x 64 tiles
@@ -128,13 +133,18 @@ __device__ __forceinline__ void gt_terms(float* x, uint32_t (&w)[P][NPAIR]) {
     }
 }
 
-// CTA (o, y) converts tiles y, y + gridDim.y, ... of operand o.  Every
+// CTA b converts tiles y, y + parts, ... of operand o, (o, y) = ctas[b]; the
+// CTAs of one operand are consecutive and the largest operands come first.
+// Every
 // thread has 16 global loads in flight per tile and writes whole 32-byte
 // sectors of the term rows.
 template <typename T, int P>
-__global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* __restrict__ ops) {
+__global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* __restrict__ ops,
+                                                               const int2* __restrict__ ctas) {
   __shared__ float tile[64][65];  // transposing mapping: tile[k][r]
-  const GtOperand op = ops[blockIdx.x];
+  const int2 cta = ctas[blockIdx.x];
+  const GtOperand op = ops[cta.x];
+  const int part = cta.y;
   const T* __restrict__ X = static_cast<const T*>(op.src);
   __nv_bfloat16* __restrict__ out = op.out;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -143,7 +153,7 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
     // K-contiguous: warp w converts rows 4w .. 4w+3 of the tile, lane l the
     // four k from 4l (and from 4l + 128 ... in later tiles)
     const int nkb = (op.Kp + 127) / 128;
-    for (int j = blockIdx.y; j < op.blocks; j += gridDim.y) {
+    for (int j = part; j < op.blocks; j += op.parts) {
       const int64_t r0 = int64_t(j / nkb) * 32 + warp * 4, k = int64_t(j % nkb) * 128 + 4 * lane;
       float v[4][4];
 #pragma unroll
@@ -175,7 +185,7 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
   // rows contiguous (sr == 1): 64 x 64 tiles through shared memory; loads
   // with lanes along r, then each thread writes 16-byte chunks (8 k) of two rows
   const int nkb = (op.Kp + 63) / 64;
-  for (int j = blockIdx.y; j < op.blocks; j += gridDim.y) {
+  for (int j = part; j < op.blocks; j += op.parts) {
     const int64_t r0 = int64_t(j / nkb) * 64, k0 = int64_t(j % nkb) * 64;
     {
       const int rr = t & 63;
