@@ -115,6 +115,26 @@ __device__ __forceinline__ void gt_ld4(const T* p, int64_t k, int64_t kend, floa
   for (int e = 0; e < 4; ++e) v[e] = k + e < kend ? gt_ld<T>(p + e) : 0.f;
 }
 
+// Four consecutive raw BF16 values of one row at p (k .. k+3, those >= kend
+// read as 0), packed two per word; no byte outside the four values is read.
+__device__ __forceinline__ uint2 gt_ld4_raw(const __nv_bfloat16* p, int64_t k, int64_t kend) {
+  const unsigned short* h = reinterpret_cast<const unsigned short*>(p);
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  if (k + 3 < kend) {
+    if ((a & 7) == 0) return __ldg(reinterpret_cast<const uint2*>(p));
+    if ((a & 3) == 0) {
+      const unsigned int* w = reinterpret_cast<const unsigned int*>(p);
+      return make_uint2(__ldg(w), __ldg(w + 1));
+    }
+    const uint32_t mid = __ldg(reinterpret_cast<const unsigned int*>(a + 2));
+    return make_uint2(uint32_t(__ldg(h)) | (mid << 16), (mid >> 16) | (uint32_t(__ldg(h + 3)) << 16));
+  }
+  uint32_t e[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) e[i] = k + i < kend ? uint32_t(__ldg(h + i)) : 0u;
+  return make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
+}
+
 // P BF16 terms of n consecutive FP32 values, t_0 = bf16(x), t_{i+1} =
 // bf16(x - t_0 - ... - t_i) (exact residuals), packed two per word; term p of
 // pair e goes to w[p][e].
@@ -155,6 +175,19 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
     const int nkb = (op.Kp + 127) / 128;
     for (int j = part; j < op.blocks; j += op.parts) {
       const int64_t r0 = int64_t(j / nkb) * 32 + warp * 4, k = int64_t(j % nkb) * 128 + 4 * lane;
+      if constexpr (sizeof(T) == 2) {
+        // BF16 is its own single term: move the raw 16-bit values
+        uint2 q[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) q[i] = (r0 + i < op.rows) ? gt_ld4_raw(X + (r0 + i) * op.sr + k, k, op.K)
+                                                              : make_uint2(0u, 0u);
+        if (k < op.Kp) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (r0 + i < op.rows) *reinterpret_cast<uint2*>(out + (r0 + i) * op.Kp + k) = q[i];
+        }
+        continue;
+      }
       float v[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -187,6 +220,35 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
   const int nkb = (op.Kp + 63) / 64;
   for (int j = part; j < op.blocks; j += op.parts) {
     const int64_t r0 = int64_t(j / nkb) * 64, k0 = int64_t(j % nkb) * 64;
+    if constexpr (sizeof(T) == 2) {
+      // BF16: transpose the raw 16-bit values (64 rows of 130 halfwords)
+      unsigned short(*th)[130] = reinterpret_cast<unsigned short(*)[130]>(&tile[0][0]);
+      const unsigned short* Xh = reinterpret_cast<const unsigned short*>(X);
+      const int rr = t & 63;
+      const int64_t r = r0 + rr;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int kk = (t >> 6) + 4 * i;
+        const int64_t k = k0 + kk;
+        th[kk][rr] = (r < op.rows && k < op.K) ? __ldg(Xh + r + k * op.sk) : (unsigned short)0;
+      }
+      __syncthreads();
+      const int c = t & 7;
+      const int64_t k = k0 + 8 * c;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int rq = (t >> 3) + 32 * h;
+        if (r0 + rq < op.rows && k < op.Kp) {
+          uint32_t w[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            w[e] = uint32_t(th[8 * c + 2 * e][rq]) | (uint32_t(th[8 * c + 2 * e + 1][rq]) << 16);
+          *reinterpret_cast<uint4*>(out + (r0 + rq) * op.Kp + k) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     {
       const int rr = t & 63;
       const int64_t r = r0 + rr;
