@@ -349,7 +349,8 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
     const GroupedProblem& p = tab[size_t(o.prob)];
     void* base;
     cuuint64_t dims[3], strides[2];
-    cuuint32_t box[3] = {cuuint32_t(kGtBK), cuuint32_t(o.which == 0 ? kGtBM : kGtBN), 1};
+    const int bk = dtype == GBBLAS_DTYPE_BF16 ? GtCfg<1>::BK : GtCfg<3>::BK;
+    cuuint32_t box[3] = {cuuint32_t(bk), cuuint32_t(o.which == 0 ? kGtBM : kGtBN), 1};
     if (o.direct) {
       base = const_cast<void*>(o.src);
       dims[0] = cuuint64_t(o.k);
@@ -379,7 +380,8 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
     }
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(&maps[size_t(2 * o.prob + o.which)], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides,
-                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
       return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: tensor map encode failed (" + std::to_string(int(r)) + ")");

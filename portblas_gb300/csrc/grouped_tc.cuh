@@ -51,10 +51,13 @@ constexpr int kGtAcc = 2;
 
 template <int P>
 struct GtCfg {
-  static constexpr int A_TILE = kGtBM * kGtBK * 2;  // 16 KB per term
-  static constexpr int B_TILE = kGtBN * kGtBK * 2;  //  8 KB per term
+  // k per stage: 64 (128-byte swizzled rows) for one or two terms, 32
+  // (64-byte swizzle) for three, so four stages fit and three are in flight
+  static constexpr int BK = P == 3 ? 32 : kGtBK;
+  static constexpr int A_TILE = kGtBM * BK * 2;  // per term
+  static constexpr int B_TILE = kGtBN * BK * 2;
   static constexpr int STAGE = P * (A_TILE + B_TILE);
-  static constexpr int STAGES = P == 1 ? 6 : (P == 2 ? 3 : 2);
+  static constexpr int STAGES = P == 1 ? 6 : (P == 2 ? 3 : 4);
   // barriers: full/empty per stage, two accumulator pairs, a work-slot pair per ring entry; then the TMEM address
   static constexpr int BARRIER_BYTES = (2 * STAGES + 2 * kGtAcc + 2 * kGtRing) * 8 + 4;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
@@ -368,7 +371,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           const Prob& pr = probs[p];
           const int local = int(tile - pr.tile_start);
           w.prob = p;
-          w.nk = pr.k > 0 ? (pr.k + kGtBK - 1) / kGtBK : 0;
+          w.nk = pr.k > 0 ? (pr.k + Cfg::BK - 1) / Cfg::BK : 0;
           // tiles of a problem go down kGtGroupM M tiles, then along N, so the
           // CTAs working at the same time share A and B panels in L2
           const int tiles_m = (pr.m + kGtBM - 1) / kGtBM;
@@ -442,8 +445,8 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           }
           tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
           uint8_t* st = smem + s * Cfg::STAGE;
-          tc::tma_load_3d(st, ma, &full[s], kb * kGtBK, w.m0, 0);
-          tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kb * kGtBK, w.n0, 0);
+          tc::tma_load_3d(st, ma, &full[s], kb * Cfg::BK, w.m0, 0);
+          tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kb * Cfg::BK, w.n0, 0);
         }
         if (!ok) break;
       }
@@ -493,10 +496,12 @@ __global__ void __launch_bounds__(kGtThreads, 1)
             for (int q = 0; q < Cfg::NPAIRS; ++q) {
               const int pa = (q == 2 || q == 4) ? 1 : (q == 5 ? 2 : 0);
               const int pb = (q == 1 || q == 4) ? 1 : (q == 3 ? 2 : 0);
-              const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
-              const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+              const uint32_t sa = tc::smem_u32(st + pa * Cfg::A_TILE);
+              const uint32_t sbb = tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE);
+              const uint64_t ad = Cfg::BK == 64 ? tc::sdesc_kmajor_sw128(sa) : tc::sdesc_kmajor_sw64(sa);
+              const uint64_t bd = Cfg::BK == 64 ? tc::sdesc_kmajor_sw128(sbb) : tc::sdesc_kmajor_sw64(sbb);
 #pragma unroll
-              for (int j = 0; j < kGtBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
+              for (int j = 0; j < Cfg::BK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
                 tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, kb != c * CHUNK || q != 0 || j != 0);
             }
             tc::mma_commit(&empty[s]);

@@ -158,6 +158,18 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
   return d;
 }
 
+// The same for the 64-byte swizzle (rows of 64 B, 8-row groups 512 B
+// apart): [32,46) stride byte offset 512 B, [61,64) layout 4 = SWIZZLE_64B.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr & 0x3FFFFu) >> 4);
+  d |= uint64_t(1) << 16;
+  d |= uint64_t(512 >> 4) << 32;
+  d |= uint64_t(1) << 46;
+  d |= uint64_t(4) << 61;
+  return d;
+}
+
 // Instruction descriptor of kind::f16 with BF16 A and B, FP32 D, both
 // operands K-major: [4,6) D format (1 = F32), [7,10) A format (1 = BF16),
 // [10,13) B format (1 = BF16), [15] / [16] A / B major (0 = K),
