@@ -111,3 +111,30 @@ def test_grouped_invalid(sb, torch_cuda):
         blas._gemm_grouped(sb, bad)
     with pytest.raises(blas.UnsupportedException):
         blas._gemm_grouped(sb, [dict(bad[0], transa="n")], dtype="float64")
+
+
+@pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
+@pytest.mark.parametrize("ta,tb", [(True, False), (False, True), (True, True), (False, False)])
+def test_grouped_bf16_aligned_operands_read_in_place(sb, torch_cuda, method, ta, tb):
+    """BF16 operands that are K-contiguous with a 16-byte-aligned leading
+    dimension are mapped by TMA in place (no conversion pass); mixed with
+    operands that need the pass, against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(53 + 2 * ta + tb)
+    probs, host = [], []
+    for i in range(24):
+        m, n, k = (int(g.integers(1, 300)) for _ in range(3))
+        # K-contiguous operands get ld rounded up to 8 elements (16 bytes)
+        lda = ((k + 7) // 8) * 8 if ta else m + int(g.integers(3))
+        ldb = ((k + 7) // 8) * 8 if not tb else n + int(g.integers(3))
+        ldc = m
+        a = torch.from_numpy(g.uniform(-1, 1, lda * (m if ta else k)).astype(np.float32)).bfloat16()
+        b = torch.from_numpy(g.uniform(-1, 1, ldb * (k if tb else n)).astype(np.float32)).bfloat16()
+        c = np.zeros(ldc * n, np.float32)
+        probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=m, n=n, k=k, alpha=1.0,
+                          a=a.cuda(), lda=lda, b=b.cuda(), ldb=ldb, beta=0.0, c=torch.from_numpy(c).cuda(), ldc=ldc))
+        host.append((ta, tb, m, n, k, 1.0, a.float().numpy(), lda, b.float().numpy(), ldb, 0.0, c, ldc))
+    blas._gemm_grouped(sb, probs, dtype="bfloat16")
+    _check(probs, host)
+    sb.check_device_error()
