@@ -333,6 +333,10 @@ gbblas_status_t gbblas_stranspose(gbblas_handle_t h, int64_t m, int64_t n, const
                                   int64_t ld_b);
 gbblas_status_t gbblas_stranspose_inplace(gbblas_handle_t h, int64_t m, int64_t n, float* a, int64_t ld_in,
                                           int64_t ld_out);
+gbblas_status_t gbblas_dtranspose(gbblas_handle_t h, int64_t m, int64_t n, const double* a, int64_t ld_a, double* b,
+                                  int64_t ld_b);
+gbblas_status_t gbblas_dtranspose_inplace(gbblas_handle_t h, int64_t m, int64_t n, double* a, int64_t ld_in,
+                                          int64_t ld_out);
 
 /* blas::extension::_reduction<op, T> (include/interface/extension_interface.h:453-462;
  *   src/interface/extension_interface.hpp:344-409, 578-593;

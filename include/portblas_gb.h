@@ -401,18 +401,26 @@ typename sb_handle_t::event_t _omatcopy(sb_handle_t& sb, char trans, index_t m, 
 template <typename element_t, typename sb_handle_t, typename index_t, typename in_t>
 typename sb_handle_t::event_t _transpose(sb_handle_t& sb, index_t m, index_t n, in_t A, index_t ld_in, index_t ld_out,
                                          const typename sb_handle_t::event_t& deps = {}) {
-  static_assert(std::is_same_v<element_t, float>, "_transpose: element type not supported");
   sb.depend(deps);
-  return sb.done(gbblas_stranspose_inplace(sb.native(), m, n, A, ld_in, ld_out));
+  if constexpr (std::is_same_v<element_t, float>)
+    return sb.done(gbblas_stranspose_inplace(sb.native(), m, n, A, ld_in, ld_out));
+  else if constexpr (std::is_same_v<element_t, double>)
+    return sb.done(gbblas_dtranspose_inplace(sb.native(), m, n, A, ld_in, ld_out));
+  else
+    throw unsupported_exception("_transpose: element type not supported");
 }
 
 /* _transpose out of place: include/interface/extension_interface.h:443-450 */
 template <typename element_t, typename sb_handle_t, typename index_t, typename in_t, typename out_t>
 typename sb_handle_t::event_t _transpose(sb_handle_t& sb, index_t m, index_t n, in_t A, index_t ld_a, out_t B,
                                          index_t ld_b, const typename sb_handle_t::event_t& deps = {}) {
-  static_assert(std::is_same_v<element_t, float>, "_transpose: element type not supported");
   sb.depend(deps);
-  return sb.done(gbblas_stranspose(sb.native(), m, n, A, ld_a, B, ld_b));
+  if constexpr (std::is_same_v<element_t, float>)
+    return sb.done(gbblas_stranspose(sb.native(), m, n, A, ld_a, B, ld_b));
+  else if constexpr (std::is_same_v<element_t, double>)
+    return sb.done(gbblas_dtranspose(sb.native(), m, n, A, ld_a, B, ld_b));
+  else
+    throw unsupported_exception("_transpose: element type not supported");
 }
 /* include/interface/extension_interface.h:453-462 */
 template <typename operator_t, typename element_t, typename sb_handle_t, typename input_t, typename output_t,

@@ -330,14 +330,15 @@ class extension:
                      _ptr(out_memory), ld_out)
 
     @staticmethod
-    def _transpose(sb_handle, m, n, A, ld_a, B=None, ld_b=None, dependencies=None):
+    def _transpose(sb_handle, m, n, A, ld_a, B=None, ld_b=None, dependencies=None, dtype=None):
         """blas::extension::_transpose: out of place (A -> B, ld_b) or, with
         B omitted and ld_b the output leading dimension, in place
         (include/interface/extension_interface.h:405-452)."""
+        p = _prefix(A, dtype)
         if B is None or isinstance(B, int) and ld_b is None:
             ld_out = B if ld_b is None else ld_b
-            return _call("gbblas_stranspose_inplace", sb_handle.handle, m, n, _ptr(A), ld_a, ld_out)
-        return _call("gbblas_stranspose", sb_handle.handle, m, n, _ptr(A), ld_a, _ptr(B), ld_b)
+            return _call(f"gbblas_{p}transpose_inplace", sb_handle.handle, m, n, _ptr(A), ld_a, ld_out)
+        return _call(f"gbblas_{p}transpose", sb_handle.handle, m, n, _ptr(A), ld_a, _ptr(B), ld_b)
 
     @staticmethod
     def _reduction(operator_t, sb_handle, buffer_in, ld, buffer_out, rows, cols, reduction_dim,

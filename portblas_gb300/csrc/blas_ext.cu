@@ -143,6 +143,20 @@ gbblas_status_t matcopy(gbblas_handle_t h, bool trans, int64_t m, int64_t n, T a
   return after_launch("matcopy");
 }
 
+// in place through one temp copy: A (m x n, ld_in) -> its transpose (ld_out)
+template <typename T>
+gbblas_status_t transpose_inplace(gbblas_handle_t h, int64_t m, int64_t n, T* a, int64_t ld_in, int64_t ld_out) {
+  if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "transpose: null handle");
+  if (m < 0 || n < 0 || ld_in < m || ld_out < n) return fail(GBBLAS_STATUS_INVALID_ARG, "transpose: bad shape");
+  if (m == 0 || n == 0) return GBBLAS_STATUS_SUCCESS;
+  if (!a) return fail(GBBLAS_STATUS_INVALID_ARG, "transpose: null matrix");
+  void* tmp;
+  GB_TRY(temp_acquire(h, sizeof(T) * size_t(m) * size_t(n), &tmp));
+  T* t = static_cast<T*>(tmp);
+  GB_TRY(matcopy<T>(h, false, m, n, T(1), a, ld_in, t, m));
+  return matcopy<T>(h, true, m, n, T(1), t, m, a, ld_out);
+}
+
 // ----------------------------------------------------------------- symm --
 // full(i, j) of an order-n symmetric matrix from the referenced triangle
 template <typename T>
@@ -282,18 +296,21 @@ gbblas_status_t gbblas_stranspose(gbblas_handle_t h, int64_t m, int64_t n, const
   clear_error();
   return matcopy<float>(h, true, m, n, 1.f, a, ld_a, b, ld_b);
 }
+gbblas_status_t gbblas_dtranspose(gbblas_handle_t h, int64_t m, int64_t n, const double* a, int64_t ld_a, double* b,
+                                  int64_t ld_b) {
+  clear_error();
+  return matcopy<double>(h, true, m, n, 1.0, a, ld_a, b, ld_b);
+}
 
 gbblas_status_t gbblas_stranspose_inplace(gbblas_handle_t h, int64_t m, int64_t n, float* a, int64_t ld_in,
                                           int64_t ld_out) {
   clear_error();
-  if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "transpose: null handle");
-  if (m < 0 || n < 0 || ld_in < m || ld_out < n) return fail(GBBLAS_STATUS_INVALID_ARG, "transpose: bad shape");
-  if (m == 0 || n == 0) return GBBLAS_STATUS_SUCCESS;
-  void* tmp;
-  GB_TRY(temp_acquire(h, sizeof(float) * size_t(m) * size_t(n), &tmp));
-  float* t = static_cast<float*>(tmp);
-  GB_TRY(matcopy<float>(h, false, m, n, 1.f, a, ld_in, t, m));
-  return matcopy<float>(h, true, m, n, 1.f, t, m, a, ld_out);
+  return transpose_inplace<float>(h, m, n, a, ld_in, ld_out);
+}
+gbblas_status_t gbblas_dtranspose_inplace(gbblas_handle_t h, int64_t m, int64_t n, double* a, int64_t ld_in,
+                                          int64_t ld_out) {
+  clear_error();
+  return transpose_inplace<double>(h, m, n, a, ld_in, ld_out);
 }
 
 gbblas_status_t gbblas_ssymm(gbblas_handle_t h, char side, char uplo, int64_t m, int64_t n, float alpha,

@@ -60,14 +60,15 @@ def test_omatcopy(sb, torch_cuda, trans, m, n, ld_in_add, ld_out_add):
     np.testing.assert_array_equal(to_host(od), oracle.omatcopy(trans, m, n, 2.0, a, ld_in, out, ld_out).astype(np.float32))
 
 
-def test_transpose_out_of_place_and_in_place(sb, torch_cuda):
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_transpose_out_of_place_and_in_place(sb, torch_cuda, dtype):
     torch = torch_cuda
     from portblas_gb300 import blas
     g = rng(5)
     m, n = 300, 77
-    a = g.uniform(-2, 5, m * n).astype(np.float32)
+    a = g.uniform(-2, 5, m * n).astype(dtype)
     ref = a.reshape(n, m).T.copy()  # m x n
-    b = torch.zeros(n * m, device="cuda")
+    b = torch.zeros(n * m, device="cuda", dtype=torch.float32 if dtype == np.float32 else torch.float64)
     blas.extension._transpose(sb, m, n, to_dev(a, torch), m, b, n)
     np.testing.assert_array_equal(to_host(b).reshape(m, n).T, ref.T)
     ad = to_dev(a, torch)
