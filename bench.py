@@ -207,12 +207,47 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev, per_op_reps=None):
         time.sleep(0.2)
     launches = blas.launch_count() - l0
     ms = start.elapsed_time(end) / steps
-    # correctness spot checks of the last step
+    # correctness of the last step against FP64 (torch, float64 on the GPU)
     iam = outs["i"].cpu().numpy()
     checks = {"iamax_index": int(iam[0]), "iamax_expected_first_planted": inp["planted"]}
     return dict(ms=ms, per_op={n: statistics.median(v) if v else None for n, v in per_op.items()},
-                launches=launches,
+                launches=launches, errors=fp64_errors(torch, inp, outs),
                 clocks=clk.summary(), checks=checks, inp=inp, outs=outs)
+
+
+def fp64_errors(torch, inp, outs):
+    """Relative error of each op's result against an FP64 computation of the
+    same inputs: vectors as max |got - ref| / max |ref|, scalars as
+    |got - ref| / |ref|, indices as an exact match with the first extreme."""
+    def vec_err(got, ref):
+        return float(((got.double() - ref).abs().max() / ref.abs().max()).item())
+
+    def sca_err(got, ref):
+        return float((abs(float(got) - float(ref)) / abs(float(ref))))
+
+    err = {}
+    A = inp["A"].view(GEMV_N, GEMV_N).double()  # A[j] = column j
+    x = inp["xg"].double()
+    err["gemv_n"] = vec_err(outs["yn"], A.T @ x)
+    err["gemv_t"] = vec_err(outs["yt"], A @ x)
+    del A
+    v, w = inp["v"].double(), inp["w"].double()
+    s = outs["s"].cpu()
+    err["asum"] = sca_err(s[0], v.abs().sum().item())
+    err["nrm2"] = sca_err(s[1], v.norm().item())
+    err["dot"] = sca_err(s[2], (v * w).sum().item())
+    av = inp["v"].abs()
+    first = lambda mask: int(torch.nonzero(mask)[0].item())
+    iam = outs["i"].cpu()
+    err["iamax"] = 0.0 if int(iam[0]) == first(av == av.max()) else 1.0
+    err["iamin"] = 0.0 if int(iam[1]) == first(av == av.min()) else 1.0
+    del v, w, av
+    R = inp["R"].view(RED_N, RED_N).double()  # R[j] = column j
+    err["reduction_inner"] = vec_err(outs["ri"], R.sum(1))
+    err["reduction_outer"] = vec_err(outs["ro"], R.sum(0))
+    del R
+    torch.cuda.empty_cache()
+    return err
 
 
 def bench_e2e(torch, blas, sb, steps, warmup, dev):
@@ -255,9 +290,8 @@ def bench_e2e(torch, blas, sb, steps, warmup, dev):
 
 def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
     """n^3 FP32 GEMM (n = 8192 by default): plain SIMT vs split-BF16 (x3 and x6
-    products), NN and TN, entries s*2^u (u ~ U[-10, 10]); error vs the FP64
-    oracle on sampled entries."""
-    import oracle
+    products), NN and TN, entries s*2^u (u ~ U[-10, 10]); error against FP64
+    dot products (torch, float64 on the GPU) on sampled entries."""
     g = np.random.default_rng(99)
 
     def pw2(size):
@@ -274,10 +308,18 @@ def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
     res = {}
     modes = [("fp32_simt", blas.sgemm_mode_t.fp32_simt), ("split_bf16x3", blas.sgemm_mode_t.split_bf16x3),
              ("split_bf16x6", blas.sgemm_mode_t.split_bf16x6)]
+    r_t = torch.from_numpy(rows).to(dev)
+    c_t = torch.from_numpy(cols).to(dev)
+    Bm = bd.view(n, n)  # Bm[j] = column j of B (column-major, ldb = n)
     for ta in (False, True):
         tag = "TN" if ta else "NN"
-        ref = oracle.gemm(ta, False, n, n, n, 1.0, a, n, b, n, 0.0, None, n, rows=rows, cols=cols)
-        scale = oracle.gemm_absscale(ta, False, n, n, n, 1.0, a, n, b, n, 0.0, None, n, rows=rows, cols=cols)
+        # row i of op(A): A is column-major n x n with lda = n
+        Am = ad.view(n, n)
+        a_rows = (Am[r_t] if ta else Am.T[r_t]).double()  # [256, n]
+        b_cols = Bm[c_t].double()                           # [256, n]
+        ref = (a_rows * b_cols).sum(1).cpu().numpy()
+        scale = (a_rows.abs() * b_cols.abs()).sum(1).cpu().numpy()
+        del a_rows, b_cols
         for name, mode in modes:
             sb.set_sgemm_mode(mode)
             try:
@@ -577,7 +619,8 @@ def main():
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)", "config": config,
         "hbm_frac_of_" + pk["src"]: value / world / pk["hbm_gbs"],
-        "per_op": {n: {"ms": t, "gbs": ab[n] / (t * 1e-3) / 1e9, "frac": ab[n] / (t * 1e-3) / 1e9 / pk["hbm_gbs"]}
+        "per_op": {n: {"ms": t, "gbs": ab[n] / (t * 1e-3) / 1e9, "frac": ab[n] / (t * 1e-3) / 1e9 / pk["hbm_gbs"],
+                       "rel_err_vs_fp64": mem["errors"].get(n)}
                    for n, t in mem["per_op"].items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "peak_src": pk["src"],
