@@ -138,3 +138,38 @@ def test_grouped_bf16_aligned_operands_read_in_place(sb, torch_cuda, method, ta,
     blas._gemm_grouped(sb, probs, dtype="bfloat16")
     _check(probs, host)
     sb.check_device_error()
+
+
+@pytest.mark.parametrize("method", METHODS, indirect=True)
+@pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
+def test_grouped_large_problems_tile_grouping(sb, torch_cuda, dtype, method):
+    """Problems with more than 8 tile rows (the scheduler walks a problem's
+    tiles in groups of 8 rows), k not a multiple of the k-block, mixed with
+    tiny ones; sampled entries against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(61)
+    shapes = [(1500, 700, 333, True, False), (1100, 1300, 97, False, True), (3, 5, 7, False, False),
+              (1025, 129, 65, True, True)]
+    probs, host = [], []
+    for (m, n, k, ta, tb) in shapes:
+        lda, ldb, ldc = (k if ta else m) + 1, (n if tb else k) + 3, m + 2
+        a = g.uniform(-1, 1, lda * (m if ta else k)).astype(np.float32)
+        b = g.uniform(-1, 1, ldb * (k if tb else n)).astype(np.float32)
+        c = g.uniform(-1, 1, ldc * n).astype(np.float32)
+        if dtype == "bfloat16":
+            a = torch.from_numpy(a).bfloat16().float().numpy()
+            b = torch.from_numpy(b).bfloat16().float().numpy()
+        tdt = torch.bfloat16 if dtype == "bfloat16" else torch.float32
+        probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=m, n=n, k=k, alpha=1.25,
+                          a=torch.from_numpy(a).to(tdt).cuda(), lda=lda, b=torch.from_numpy(b).to(tdt).cuda(),
+                          ldb=ldb, beta=0.5, c=torch.from_numpy(c).cuda(), ldc=ldc))
+        host.append((ta, tb, m, n, k, a, lda, b, ldb, c, ldc))
+    blas._gemm_grouped(sb, probs, dtype=dtype)
+    for p, (ta, tb, m, n, k, a, lda, b, ldb, c, ldc) in zip(probs, host):
+        rows = g.integers(0, m, 64)
+        cols = g.integers(0, n, 64)
+        ref = oracle.gemm(ta, tb, m, n, k, 1.25, a, lda, b, ldb, 0.5, c, ldc, rows=rows, cols=cols)
+        got = p["c"].cpu().numpy().reshape(n, ldc).T[rows, cols]
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * max(1, k))
+    sb.check_device_error()
