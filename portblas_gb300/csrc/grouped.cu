@@ -1,5 +1,6 @@
-// grouped.cu — grouped GEMM over uneven problems: one persistent launch with
-// a device-side tile scheduler, replayed through a CUDA graph.
+// grouped.cu — grouped GEMM over uneven problems: a persistent launch with a
+// device-side tile scheduler (preceded, on the tensor-core path, by one
+// operand-conversion pass), captured once and replayed as a CUDA graph.
 //
 // portBLAS has only uniform batches (_gemm_batched / _gemm_strided_batched,
 // src/interface/gemm_interface.hpp:200-240, with Gemm's batch loop in
@@ -15,9 +16,11 @@
 // on another.  The last CTA to finish resets the counters, so the same launch
 // can be replayed from a CUDA graph with no host work.
 //
-// Tile compute: A and B slabs (BK = 16) are converted from FP32 or BF16 to
-// FP32 as they are staged in shared memory (any transpose), and each of 256
-// threads accumulates a 4x4 FP32 register tile.
+// Two tile methods: the tcgen05 path of grouped_tc.cuh (default: 128 x 128
+// tiles, BF16-term operands streamed by per-operand TMA maps), and a SIMT
+// path (GBBLAS_GROUPED_METHOD=simt: 64 x 64 tiles; A and B slabs, BK = 16,
+// converted to FP32 as they are staged in shared memory, any transpose; each
+// of 256 threads accumulates a 4x4 FP32 register tile).
 #include <cuda_bf16.h>
 
 #include <algorithm>
