@@ -94,6 +94,12 @@ gbblas_status_t gbblas_wait(gbblas_handle_t handle);
 gbblas_status_t gbblas_temp_bytes(gbblas_handle_t handle, size_t* bytes);
 /* Reads and clears the device-side error word (bounded waits that gave up). */
 gbblas_status_t gbblas_check_device_error(gbblas_handle_t handle);
+/* No portBLAS counterpart: self-test of the device error path.  Launches one
+ * CTA that waits on an mbarrier nothing ever arrives at, with the given wall
+ * clock limit (capped at 1 s); the wait gives up, records its code in the
+ * handle's error word and the kernel returns, leaving the context usable.
+ * gbblas_check_device_error then reports GBBLAS_STATUS_TIMEOUT. */
+gbblas_status_t gbblas_selftest_wait_timeout(gbblas_handle_t handle, uint64_t limit_ns);
 const char* gbblas_status_string(gbblas_status_t status);
 /* Message of the last failing call on this thread ("" if none). */
 const char* gbblas_last_error(void);

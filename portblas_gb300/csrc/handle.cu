@@ -8,6 +8,7 @@
 #include <new>
 
 #include "common.cuh"
+#include "tc_ptx.cuh"
 
 namespace gb {
 
@@ -50,6 +51,19 @@ gbblas_status_t temp_acquire(gbblas_handle_t h, size_t bytes, void** ptr) {
   }
   *ptr = h->temp;
   return GBBLAS_STATUS_SUCCESS;
+}
+
+// Waits on an mbarrier that never completes (phase 0, no arrivals) until the
+// bounded wait gives up, then records the error code and returns.
+constexpr int kErrSelftest = 901;
+__global__ void selftest_timeout_kernel(int* err, uint64_t limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !tc::mbar_wait(&bar, 0, limit_ns)) atomicExch(err, kErrSelftest);
 }
 
 }  // namespace gb
@@ -150,6 +164,14 @@ gbblas_status_t gbblas_check_device_error(gbblas_handle_t h) {
     return fail(GBBLAS_STATUS_TIMEOUT, "a bounded device-side wait gave up (code " + std::to_string(flag) + ")");
   }
   return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status_t gbblas_selftest_wait_timeout(gbblas_handle_t h, uint64_t limit_ns) {
+  clear_error();
+  if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "selftest: null handle");
+  if (limit_ns > 1000000000ull) limit_ns = 1000000000ull;
+  selftest_timeout_kernel<<<1, 32, 0, h->stream>>>(h->dev_error, limit_ns);
+  return after_launch("selftest_timeout");
 }
 
 gbblas_status_t gbblas_set_sgemm_mode(gbblas_handle_t h, int mode) {
