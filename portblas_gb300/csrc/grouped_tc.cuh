@@ -354,15 +354,18 @@ __global__ void __launch_bounds__(kGtThreads, 1)
 
   if (warp == 2) {
     // ----------------------------------------------------------- scheduler --
-    // kGtBatch tiles per atomic; their lookups run in parallel on the lanes
+    // kGtBatch tiles per atomic (their lookups run in parallel on the
+    // lanes) until the last two rounds of the grid, then one at a time so the
+    // CTAs finish together
     __shared__ GtWork batch[kGtBatch];
     uint32_t i = 0;
+    int take = kGtBatch;
     bool more = true;
     while (more) {
       long long base = 0;
-      if (lane == 0) base = (long long)atomicAdd(&counters[0], (unsigned long long)kGtBatch);
+      if (lane == 0) base = (long long)atomicAdd(&counters[0], (unsigned long long)take);
       base = __shfl_sync(0xffffffffu, base, 0);
-      if (lane < kGtBatch) {
+      if (lane < take) {
         const long long tile = base + lane;
         GtWork w{};
         w.prob = -1;
@@ -395,7 +398,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       }
       __syncwarp();
       if (lane == 0) {
-        for (int l = 0; l < kGtBatch; ++l, ++i) {
+        for (int l = 0; l < take; ++l, ++i) {
           const int r = i % kGtRing;
           if (!tc::mbar_wait(&wempty[r], ((i / kGtRing) & 1) ^ 1)) {
             atomicExch(err, kErrGtProducer);
@@ -411,6 +414,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         }
       }
       more = __shfl_sync(0xffffffffu, more, 0);
+      if (base + 2ll * kGtBatch * gridDim.x >= total_tiles) take = 1;
       __syncwarp();
     }
   } else if (warp == 0) {
