@@ -228,12 +228,15 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
       unsigned short(*th)[130] = reinterpret_cast<unsigned short(*)[130]>(&tile[0][0]);
       const unsigned short* Xh = reinterpret_cast<const unsigned short*>(X);
       const int rr = t & 63;
-      const int64_t r = r0 + rr;
+      const bool row_ok = r0 + rr < op.rows;
+      // column k0 + kk of this thread's row; the next column is 4 * sk on
+      const int kq = (t >> 6);
+      const unsigned short* q = Xh + (row_ok ? r0 + rr : 0) + (k0 + kq) * op.sk;
+      const int64_t step = 4 * op.sk;
+      const int64_t kleft = op.K - k0 - kq;  // columns of this thread still inside K, from i = 0
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
-        const int kk = (t >> 6) + 4 * i;
-        const int64_t k = k0 + kk;
-        th[kk][rr] = (r < op.rows && k < op.K) ? __ldg(Xh + r + k * op.sk) : (unsigned short)0;
+        th[kq + 4 * i][rr] = (row_ok && 4 * i < kleft) ? __ldg(q + i * step) : (unsigned short)0;
       }
       __syncthreads();
       const int c = t & 7;
@@ -254,12 +257,14 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
     }
     {
       const int rr = t & 63;
-      const int64_t r = r0 + rr;
+      const bool row_ok = r0 + rr < op.rows;
+      const int kq = (t >> 6);
+      const T* q = X + (row_ok ? r0 + rr : 0) + (k0 + kq) * op.sk;
+      const int64_t step = 4 * op.sk;
+      const int64_t kleft = op.K - k0 - kq;
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
-        const int kk = (t >> 6) + 4 * i;
-        const int64_t k = k0 + kk;
-        tile[kk][rr] = (r < op.rows && k < op.K) ? gt_ld<T>(X + r + k * op.sk) : 0.f;
+        tile[kq + 4 * i][rr] = (row_ok && 4 * i < kleft) ? gt_ld<T>(q + i * step) : 0.f;
       }
     }
     __syncthreads();
