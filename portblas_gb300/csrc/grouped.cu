@@ -553,6 +553,8 @@ gbblas_status_t gbblas_grouped_plan_run(gbblas_handle_t h, gbblas_grouped_plan_t
   clear_error();
   if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "grouped: null handle");
   if (!plan) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: null plan");
+  if (plan->device != h->device)
+    return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: the plan belongs to another device than the handle");
   if (plan->total_tiles == 0) return GBBLAS_STATUS_SUCCESS;
   if (!plan->exec) {
     // capture the launch once on a private stream (the handle's stream may be
