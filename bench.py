@@ -377,7 +377,7 @@ def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
 
 
 def bench_batched(torch, blas, sb, dev, reps=10):
-    """BASELINE config 4: a grouped batch of 2048 problems with M, N, K each
+    """Batching workload: a grouped batch of 2048 problems with M, N, K each
     log-uniform in [16, 512] (seeded), random transposes, FP32 and BF16 inputs
     (FP32 accumulate), as one persistent launch replayed from a CUDA graph;
     and a strided batch of 4096 x 64^3 FP32."""
@@ -439,7 +439,7 @@ def bench_batched(torch, blas, sb, dev, reps=10):
 
 
 def bench_selector(torch, blas, sb, dev, shapes=48):
-    """BASELINE config 5 spot check: regret of the learned selector and of the
+    """Learned-selector spot check: regret of the learned selector and of the
     size heuristic against exhaustive timing on fresh seeded shapes (the full
     1000-shape held-out evaluation is in tuning/sgemm_selector_report.json)."""
     import ctypes as C
