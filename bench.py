@@ -201,11 +201,14 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev, record_ops=True):
     torch.cuda.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
         time.sleep(0.3)
+        barrier(torch)
+        torch.cuda.synchronize()
         start.record()
         for k in range(steps):
             run_step(blas, sb, inp, outs, {dom: dom_ev[k]} if record_ops else None)
         end.record()
         torch.cuda.synchronize()
+        barrier(torch)
         time.sleep(0.2)
     launches = blas.launch_count() - l0
     ms = start.elapsed_time(end) / steps
@@ -216,6 +219,24 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev, record_ops=True):
     return dict(ms=ms, per_op={n: statistics.median(v) if v else None for n, v in per_op.items()},
                 dom=dom, dom_ms=dom_ms, launches=launches, errors=fp64_errors(torch, inp, outs),
                 clocks=clk.summary(), checks=checks, inp=inp, outs=outs)
+
+
+def barrier(torch) -> None:
+    """All ranks meet here when the job is distributed (no-op on one process)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def max_over_ranks(torch, values, dev):
+    """Element-wise maximum of per-rank values (every rank must call it); the
+    values themselves on one process."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
 
 
 def fp64_errors(torch, inp, outs):
@@ -283,11 +304,14 @@ def bench_e2e(torch, blas, sb, steps, warmup, dev):
         step()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(torch)
+    torch.cuda.synchronize()
     start.record()
     for _ in range(steps):
         step()
     end.record()
     torch.cuda.synchronize()
+    barrier(torch)
     return dict(ms=start.elapsed_time(end) / steps, h2d=h2d, d2h=d2h)
 
 
@@ -597,13 +621,7 @@ def main():
     mem = bench_memory_set(torch, blas, sb, args.steps, warmup, dev)
     e2e = bench_e2e(torch, blas, sb, max(3, args.steps // 4), 3, dev)
     ms = mem["ms"]
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms, e2e["ms"]], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
-    else:
-        e2e_ms = e2e["ms"]
+    ms, e2e_ms = max_over_ranks(torch, [ms, e2e["ms"]], dev)
     value = world * total_bytes / (ms * 1e-3) / 1e9
     pk = peaks()
     ab = algorithmic_bytes()
