@@ -434,7 +434,8 @@ def bench_batched(torch, blas, sb, dev, reps=10):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         out["grouped"][dt] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
-                              "gbs": bytes_in / (ms * 1e-3) / 1e9, "bytes_per_call": bytes_in}
+                              "gbs": bytes_in / (ms * 1e-3) / 1e9, "bytes_per_call": bytes_in,
+                              "max_norm_err_vs_fp64": grouped_error(torch, probs[::128])}
         plan.close()
         del probs
     # strided batch 4096 x 64^3 FP32 (A, B, C 64 MiB each)
@@ -455,11 +456,38 @@ def bench_batched(torch, blas, sb, dev, reps=10):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    ref = (A[: n * n].view(n, n).T.double() @ B[: n * n].view(n, n).T.double())
-    err = float((Cc[: n * n].view(n, n).T.double() - ref).abs().max().item())
+    errs = []
+    for i in (0, nb // 2, nb - 1):  # |A||B|-normalised error of three problems against FP64
+        Ai = A[i * n * n:(i + 1) * n * n].view(n, n).T.double()
+        Bi = B[i * n * n:(i + 1) * n * n].view(n, n).T.double()
+        ref = Ai @ Bi
+        scale = Ai.abs() @ Bi.abs()
+        errs.append(float(((Cc[i * n * n:(i + 1) * n * n].view(n, n).T.double() - ref).abs() / scale).max().item()))
     out["strided_4096x64"] = {"ms": ms, "tflops": f / (ms * 1e-3) / 1e12, "gbs": byt / (ms * 1e-3) / 1e9,
-                              "max_abs_err_first": err}
+                              "max_norm_err_vs_fp64": max(errs)}
     return out
+
+
+def grouped_error(torch, probs):
+    """Largest |A||B|-normalised error of the given grouped problems (column-
+    major, alpha = 1, beta = 0) against FP64 products on the GPU."""
+    worst = 0.0
+    for p in probs:
+        m, n, k = p["m"], p["n"], p["k"]
+        # column-major storage: op(A) is m x k, op(B) is k x n
+        if p["transa"] == "n":
+            a = p["a"].double().view(k, p["lda"])[:, :m].T
+        else:
+            a = p["a"].double().view(m, p["lda"])[:, :k]
+        if p["transb"] == "n":
+            b = p["b"].double().view(n, p["ldb"])[:, :k].T
+        else:
+            b = p["b"].double().view(k, p["ldb"])[:, :n]
+        ref = a @ b
+        scale = a.abs() @ b.abs()
+        got = p["c"].double().view(n, p["ldc"]).T[:m]
+        worst = max(worst, float(((got - ref).abs() / scale.clamp_min(1e-300)).max().item()))
+    return worst
 
 
 def bench_selector(torch, blas, sb, dev, shapes=48):
