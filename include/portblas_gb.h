@@ -4,10 +4,11 @@
  *
  * Source written against portBLAS compiles unchanged for these calls: the
  * function names, template shapes, argument order and meaning follow
- *   include/interface/blas1_interface.h   (_asum, _nrm2, _dot, _iamax, _iamin)
+ *   include/interface/blas1_interface.h   (_asum, _nrm2, _dot, _iamax, _iamin,
+ *                                          _scal, _axpy, _copy, _sdsdot)
  *   include/interface/blas2_interface.h   (_gemv)
- *   include/interface/blas3_interface.h   (_gemm, _gemm_batched, _gemm_strided_batched)
- *   include/interface/extension_interface.h (extension::_reduction)
+ *   include/interface/blas3_interface.h   (_gemm, _gemm_batched, _gemm_strided_batched, _symm)
+ *   include/interface/extension_interface.h (extension::_reduction, _omatcopy, _transpose)
  * and the errors are the same exception types (std::invalid_argument,
  * blas::unsupported_exception).  Differences a caller can observe:
  *   - SB_Handle wraps a cudaStream_t instead of a sycl::queue, and buffers are
