@@ -188,17 +188,18 @@ using namespace gb;
 
 template <typename T, int P>
 static gbblas_status_t launch_grouped_tc(cudaStream_t s, gbblas_grouped_plan_s* p, int* err) {
+  constexpr int kChunk = kGtChunkK / GtCfg<P>::BK;  // k-blocks per TMEM chunk
   if (p->n_ops > 0) {
     grouped_split_kernel<T, P><<<unsigned(p->n_ctas), 256, 0, s>>>(p->ops, p->ctas);
     GB_TRY(after_launch("grouped_split"));
   }
   static bool attr = false;
   if (!attr) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<P, kGtChunk, GroupedProblem>,
+    GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<P, kChunk, GroupedProblem>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<P>::SMEM));
     attr = true;
   }
-  grouped_tc_kernel<P, kGtChunk, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
+  grouped_tc_kernel<P, kChunk, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
       p->table, p->tile_prob, p->maps, p->total_tiles, p->counters, err);
   return after_launch("grouped_tc");
 }

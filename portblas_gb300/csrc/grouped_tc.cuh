@@ -45,7 +45,10 @@ namespace gb {
 
 // Warps: 0 producer, 1 MMA issuer, 2 scheduler, 3..10 epilogue.
 constexpr int kGtBM = 128, kGtBN = 128, kGtBK = 64, kGtEpiWarps = 8, kGtThreads = 32 * (3 + kGtEpiWarps),
-              kGtChunk = 8, kGtRing = 8, kGtGroupM = 8;
+              kGtRing = 8, kGtGroupM = 8;
+// K depth of one TMEM chunk before its promotion into FP32 registers (a
+// shallower chunk keeps more of the sum in FP32; 128 costs no time here)
+constexpr int kGtChunkK = 128;
 // TMEM chunk accumulators (the MMA warp runs up to kGtAcc - 1 chunks ahead of the epilogue)
 constexpr int kGtAcc = 2;
 
