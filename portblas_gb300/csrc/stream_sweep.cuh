@@ -26,7 +26,7 @@ constexpr int kStConsumers = 8;                       // consumer warps
 constexpr int kStThreads = (kStConsumers + 1) * 32;   // + one producer warp
 constexpr int kStTileBytes = 16384;
 
-enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203 };
+enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203, kErrSweepX = 204 };
 
 // x elements staged in shared memory by the rows sweep (one column split)
 constexpr int64_t kRowsXStage = 8192;
@@ -43,6 +43,49 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
       ::"r"(tc::smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(tc::smem_u32(bar)), "r"(c0), "r"(c1)
       : "memory");
 }
+
+// Staging of x (n elements from src with stride inc) into shared memory xs,
+// zero-filled up to `fill` elements.  With unit stride and a 16-byte-aligned
+// src the 16-byte-aligned bulk of x is one cp.async.bulk copy issued by the
+// producer warp at kernel start (so it travels with the first tiles of A);
+// the consumers copy the rest with several loads in flight per thread.
+template <typename T>
+struct XStage {
+  int64_t n, fill, inc;
+  const T* src;
+  uint32_t bulk;  // elements covered by the bulk copy (0: none)
+  __device__ XStage(const T* src_, int64_t n_, int64_t fill_, int64_t inc_) : n(n_), fill(fill_), inc(inc_), src(src_) {
+    constexpr int64_t V = 16 / int64_t(sizeof(T));
+    const bool ok = inc == 1 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+    bulk = ok ? uint32_t(n / V * V) : 0u;
+  }
+  // producer lane: issue the bulk part
+  __device__ void issue(T* xs, uint64_t* bar) const {
+    if (bulk == 0) return;
+    tc::mbar_arrive_expect_tx(bar, bulk * uint32_t(sizeof(T)));
+    tc::bulk_load_1d(xs, src, bulk * uint32_t(sizeof(T)), bar);
+  }
+  // consumer threads (tid in [0, nthreads)): the rest, then wait for the bulk
+  // part; false if that wait gave up
+  template <int NTHREADS>
+  __device__ bool finish(T* xs, uint64_t* bar, int tid) const {
+    constexpr int U = 4;
+    for (int64_t b = int64_t(bulk); b < fill; b += int64_t(U) * NTHREADS) {
+      T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = b + tid + int64_t(u) * NTHREADS;
+        v[u] = i < n ? src[i * inc] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = b + tid + int64_t(u) * NTHREADS;
+        if (i < fill) xs[i] = v[u];
+      }
+    }
+    return bulk == 0 || tc::mbar_wait(bar, 0);
+  }
+};
 
 // Producer loop shared by both sweeps: tile t of `ntiles` at coordinates
 // (x0 + t*dx, y0 + t*dy).  Returns after every issued copy has landed.
@@ -87,8 +130,10 @@ __global__ void __launch_bounds__(kStThreads)
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
   uint64_t* empty = full + kStStages;
-  Acc* red = reinterpret_cast<Acc*>(empty + kStStages);  // [kStConsumers][BM]
-  T* xs = reinterpret_cast<T*>(red + kStConsumers * BM);  // [cols_per_split] when staged
+  uint64_t* xbar = empty + kStStages;
+  Acc* red = reinterpret_cast<Acc*>(xbar + 1);  // [kStConsumers][BM]
+  T* xs = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(red + kStConsumers * BM) + 15) &
+                               ~uintptr_t(15));  // [cols_per_split] when staged
   __shared__ bool is_last;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -102,24 +147,30 @@ __global__ void __launch_bounds__(kStThreads)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], kStConsumers);
     }
+    tc::mbar_init(xbar, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
 
+  // x of this column split goes to shared memory while the first tiles land
+  const bool xstaged = HAS_X && cols_per_split <= kRowsXStage;
+  const XStage<T> xst(HAS_X ? xb + c0 * incx : xb, c1 - c0, c1 - c0, incx);
   if (warp == kStConsumers) {
-    if (lane == 0)
+    if (lane == 0) {
+      if (xstaged) xst.issue(xs, xbar);
       sweep_producer<kStTileBytes>(&tmA, ring, full, empty, ntiles, int32_t(r0), 0, int32_t(c0), BC, err);
+    }
   } else {
-    // x of this column split goes to shared memory while the first tiles land
-    const bool xstaged = HAS_X && cols_per_split <= kRowsXStage;
+    bool ok = true;
     if (xstaged) {
-      for (int64_t i = threadIdx.x; i < c1 - c0; i += kStConsumers * 32) xs[i] = xb[(c0 + i) * incx];
+      ok = xst.template finish<kStConsumers * 32>(xs, xbar, threadIdx.x);
+      if (!ok && threadIdx.x == 0) atomicExch(err, kErrSweepX);
       consumers_sync();
     }
     Acc acc[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
-    for (int t = 0; t < ntiles; ++t) {
+    for (int t = 0; t < (ok ? ntiles : 0); ++t) {
       const int s = t % kStStages;
       if (!tc::mbar_wait(&full[s], (t / kStStages) & 1)) {
         if (lane == 0) atomicExch(err, kErrSweepFull);
@@ -194,7 +245,8 @@ __global__ void __launch_bounds__(kStThreads)
   uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStStages * kStTileBytes);
   uint64_t* empty = full + kStStages;
-  T* xs = reinterpret_cast<T*>(empty + kStStages);  // [rows_per_split] when HAS_X
+  uint64_t* xbar = empty + kStStages;
+  T* xs = reinterpret_cast<T*>(xbar + 2);  // [rows_per_split] when HAS_X (16-byte aligned)
   __shared__ unsigned long long last_mask;  // bit c: this CTA folds column tile ct0 + c
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -208,12 +260,16 @@ __global__ void __launch_bounds__(kStThreads)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], kStConsumers);
     }
+    tc::mbar_init(xbar, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
 
+  // the chunk's x (zero past the matrix) is staged while the first tiles land
+  const XStage<T> xst(HAS_X ? xb + r0 * incx : xb, rlen, int64_t(nrt) * BR, incx);
   if (warp == kStConsumers) {
     if (lane == 0) {
+      if (HAS_X) xst.issue(xs, xbar);
       // tile t: column tile t / nrt, row tile t % nrt
       tc::tma_prefetch_desc(&tmA);
       const int ntiles = nct * nrt;
@@ -236,12 +292,12 @@ __global__ void __launch_bounds__(kStThreads)
         }
     }
   } else {
+    bool ok = true;
     if (HAS_X) {
-      for (int64_t i = threadIdx.x; i < int64_t(nrt) * BR; i += kStConsumers * 32)
-        xs[i] = i < rlen ? xb[(r0 + i) * incx] : T(0);
+      ok = xst.template finish<kStConsumers * 32>(xs, xbar, threadIdx.x);
+      if (!ok && threadIdx.x == 0) atomicExch(err, kErrSweepX);
       consumers_sync();
     }
-    bool ok = true;
     for (int c = 0; c < nct && ok; ++c) {
       Acc acc[CPW];
 #pragma unroll
@@ -341,12 +397,12 @@ inline bool make_matrix_map(CUtensorMap* map, const T* base, int64_t M, int64_t 
 // Smem bytes of the two sweeps (ring + barriers + per-kernel extras + align slack).
 template <typename Acc, typename T>
 constexpr size_t rows_tma_smem(bool has_x) {
-  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + sizeof(Acc) * kStConsumers * 32 * (16 / sizeof(T)) +
-         (has_x ? sizeof(T) * size_t(kRowsXStage) : 0);
+  return 128 + kStStages * kStTileBytes + (2 * kStStages + 1) * 8 +
+         sizeof(Acc) * kStConsumers * 32 * (16 / sizeof(T)) + 16 + (has_x ? sizeof(T) * size_t(kRowsXStage) : 0);
 }
 template <typename T>
 inline size_t cols_tma_smem(bool has_x, int64_t rows_per_split) {
-  return 128 + kStStages * kStTileBytes + 2 * kStStages * 8 + (has_x ? sizeof(T) * size_t(rows_per_split) : 0);
+  return 128 + kStStages * kStTileBytes + (2 * kStStages + 2) * 8 + (has_x ? sizeof(T) * size_t(rows_per_split) : 0);
 }
 
 struct TmaPlan {
