@@ -465,6 +465,66 @@ def bench_batched(torch, blas, sb, dev, reps=10):
         errs.append(float(((Cc[i * n * n:(i + 1) * n * n].view(n, n).T.double() - ref).abs() / scale).max().item()))
     out["strided_4096x64"] = {"ms": ms, "tflops": f / (ms * 1e-3) / 1e12, "gbs": byt / (ms * 1e-3) / 1e9,
                               "max_norm_err_vs_fp64": max(errs)}
+    out["grouped_splitk"] = bench_grouped_splitk(torch, blas, sb, dev, reps)
+    return out
+
+
+SPLITK_CASES = {
+    "tall_skinny_48x48x2^18": [(48, 48, 1 << 18)],
+    "4x_128x128x65536": [(128, 128, 65536)] * 4,
+    "16x_256x256x32768": [(256, 256, 32768)] * 16,
+    "2_long_64_short": [(200, 130, 40000), (64, 64, 100000)] + [(100, 100, 200)] * 64,
+}
+
+
+def bench_grouped_splitk(torch, blas, sb, dev, reps=10):
+    """Long-K grouped batches (few output tiles, K up to 2^18): the plan's
+    split-K schedule against the same plan with split-K off
+    (GBBLAS_GROUPED_SPLITK=0), FP32 and BF16 inputs, uniform [0, 1) data;
+    error of the first problem against FP64."""
+    out = {}
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    for dt in ("bfloat16", "float32"):
+        tdt = torch.float32 if dt == "float32" else torch.bfloat16
+        for name, shapes in SPLITK_CASES.items():
+            probs = []
+            for (m, n, k) in shapes:
+                a = torch.rand(m * k, device=dev, generator=g).to(tdt)
+                b = torch.rand(k * n, device=dev, generator=g).to(tdt)
+                probs.append(dict(transa="n", transb="n", m=m, n=n, k=k, alpha=1.0, a=a, lda=m, b=b, ldb=k,
+                                  beta=0.0, c=torch.empty(m * n, device=dev), ldc=m))
+            flop = sum(2.0 * m * n * k for (m, n, k) in shapes)
+            res = {}
+            for mode in ("split", "no_split"):
+                old = os.environ.get("GBBLAS_GROUPED_SPLITK")
+                os.environ["GBBLAS_GROUPED_SPLITK"] = "1" if mode == "split" else "0"
+                try:
+                    plan = blas.GroupedPlan(sb, probs, dtype=dt)
+                finally:
+                    if old is None:
+                        del os.environ["GBBLAS_GROUPED_SPLITK"]
+                    else:
+                        os.environ["GBBLAS_GROUPED_SPLITK"] = old
+                tiles, splits = plan.info()
+                for _ in range(3):
+                    plan.run()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    plan.run()
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                m, n, k = shapes[0]
+                p = probs[0]
+                ref = p["a"].double().view(k, m).T @ p["b"].double().view(n, k).T
+                err = float(((p["c"].double().view(n, m).T - ref).abs() / ref.abs()).max().item())
+                res[mode] = {"ms": ms, "tflops": flop / (ms * 1e-3) / 1e12, "tiles": tiles, "max_splits": splits,
+                             "max_rel_err_vs_fp64": err}
+                plan.close()
+            out[f"{dt}:{name}"] = res
     return out
 
 

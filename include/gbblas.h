@@ -324,6 +324,18 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
                                            gbblas_grouped_plan_t* plan);
 gbblas_status_t gbblas_grouped_plan_run(gbblas_handle_t h, gbblas_grouped_plan_t plan);
 gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t plan);
+/* No portBLAS counterpart: the plan's schedule.  `tiles`: tiles the
+ * persistent kernel hands out (output tiles x K slices); `max_splits`: the
+ * largest number of K slices of any problem (1: no split-K).  Either output
+ * pointer may be null. */
+gbblas_status_t gbblas_grouped_plan_info(gbblas_grouped_plan_t plan, int64_t* tiles, int* max_splits);
+/* No portBLAS counterpart: the tile schedule a tcgen05 grouped plan of these
+ * problems would use on a GPU with `sm_count` SMs, computed on the host (no
+ * device call).  `tiles`: tiles handed out; `splits[i]` (host array of
+ * `count`): K slices of problem i, 0 for a problem with m or n == 0. */
+gbblas_status_t gbblas_grouped_schedule(int dtype, int64_t count, const char* transa, const char* transb,
+                                        const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
+                                        int sm_count, int64_t* tiles, int* splits);
 
 /* ------------------------------------------------------------ extension -- */
 /* blas::extension::_omatcopy (include/interface/extension_interface.h:188-198):

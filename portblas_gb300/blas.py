@@ -391,6 +391,26 @@ def _gemm_grouped(sb_handle, problems, dtype="float32"):
     return _call("gbblas_gemm_grouped", sb_handle.handle, _dtype_code(dtype), *args)
 
 
+def grouped_schedule(problems, dtype="float32", sm_count=152):
+    """Host-side tile schedule of a tcgen05 grouped GEMM over ``problems``
+    (dicts with transa, transb, m, n, k, alpha) on a GPU with ``sm_count``
+    SMs: (tiles handed out, K slices per problem; 0 for an empty problem)."""
+    L = _lib.load()
+    cnt = len(problems)
+    I64 = C.c_int64 * max(cnt, 1)
+    F32 = C.c_float * max(cnt, 1)
+    ta = C.create_string_buffer(bytes(_ch(p["transa"])[0] for p in problems), max(cnt, 1))
+    tb = C.create_string_buffer(bytes(_ch(p["transb"])[0] for p in problems), max(cnt, 1))
+    m, n, k = (I64(*[p[key] for p in problems]) for key in ("m", "n", "k"))
+    alpha = F32(*[p["alpha"] for p in problems])
+    tiles = C.c_int64()
+    splits = (C.c_int * max(cnt, 1))()
+    _check(L.gbblas_grouped_schedule(_dtype_code(dtype), cnt, C.addressof(ta), C.addressof(tb), C.addressof(m),
+                                     C.addressof(n), C.addressof(k), C.addressof(alpha), int(sm_count),
+                                     C.byref(tiles), C.addressof(splits)))
+    return tiles.value, list(splits)[:cnt]
+
+
 class GroupedPlan:
     """A reusable grouped GEMM replayed from a CUDA graph
     (gbblas_grouped_plan_create / _run / _destroy)."""
@@ -406,6 +426,12 @@ class GroupedPlan:
     def run(self):
         _check(self._L.gbblas_grouped_plan_run(self.sb.handle, self._p))
         return []
+
+    def info(self):
+        """(tiles handed out, largest number of K slices of any problem)."""
+        tiles, splits = C.c_int64(), C.c_int()
+        _check(self._L.gbblas_grouped_plan_info(self._p, C.byref(tiles), C.byref(splits)))
+        return tiles.value, splits.value
 
     def close(self):
         if getattr(self, "_p", None) is not None and self._p.value:

@@ -24,6 +24,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -50,6 +51,11 @@ struct GroupedProblem {
   const void* b;
   float* c;
   int64_t lda, ldb, ldc;
+  // split-K (tcgen05 tiles): K slices per output tile, k-blocks per slice,
+  // and the problem's first partial float / ticket in the launch's arrays
+  int splits, kbs;
+  int64_t part_off, tick_off;
+  int64_t src;  // index of the problem in the caller's arrays
 };
 
 constexpr int kGT = 64, kGK = 16, kGThreads = 256;
@@ -179,7 +185,10 @@ struct gbblas_grouped_plan_s {
   int n_ops = 0;
   int2* ctas = nullptr;  // (operand, part) of each split-pass CTA
   int n_ctas = 0;
+  float* parts = nullptr;         // split-K partial blocks
+  unsigned int* ticks = nullptr;  // split-K tickets (zero between launches)
   cudaGraphExec_t exec = nullptr;
+  int max_splits = 1;
   int device = 0;
   int* err = nullptr;  // device error word of the creating handle
 };
@@ -200,7 +209,7 @@ static gbblas_status_t launch_grouped_tc(cudaStream_t s, gbblas_grouped_plan_s* 
     attr = true;
   }
   grouped_tc_kernel<P, kChunk, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
-      p->table, p->tile_prob, p->maps, p->total_tiles, p->counters, err);
+      p->table, p->tile_prob, p->maps, p->total_tiles, p->counters, p->parts, p->ticks, err);
   return after_launch("grouped_tc");
 }
 
@@ -229,12 +238,101 @@ extern "C" gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t pla
   return GBBLAS_STATUS_SUCCESS;
 }
 
+// ------------------------------------------------------------ split-K plan --
+// The persistent kernel hands out tiles longest first (list scheduling), so
+// its makespan is at least the longest tile.  When one problem's tiles are
+// much longer (in K) than the mean work per SM (a few tall-skinny or long-K
+// problems), their K is cut into slices.  A slice costs its k-blocks; the
+// last slice of a tile also folds all S partials, about f k-blocks each
+// (f = 4 for BF16 inputs, 3 for FP32 inputs, whose k-blocks carry six term
+// products), so one tile of nk k-blocks is fastest near S = sqrt(nk / f).
+// Slices stay at least kGtMinSliceK deep, S <= kGtMaxSplits, and the tiles
+// of the whole launch are kept within one wave of sm_count CTAs by halving
+// the largest S first (more tiles than CTAs was measured slower: each extra
+// round re-reads operand panels and the folds queue up).
+constexpr int kGtMaxSplits = 64;
+constexpr int64_t kGtMinSliceK = 256;
+
+// K slices of a tile of nk k-blocks under a cap of `cap` k-blocks per slice:
+// splits >= 1 always (an empty K, alpha == 0, is one slice of nothing).
+static void slice_shape(int64_t nk, int64_t cap, int& splits, int& kbs) {
+  if (nk <= cap || nk <= 1 || cap < 1) {
+    splits = 1;
+    kbs = int(nk);
+    return;
+  }
+  const int64_t sp = std::min<int64_t>(cdiv(nk, cap), kGtMaxSplits);
+  const int64_t len = cdiv(nk, sp);
+  splits = int(cdiv(nk, len));
+  kbs = int(len);
+}
+
+// Sets splits / kbs of every problem (k-blocks of `bk` elements; f as above).
+static void plan_splits(std::vector<GroupedProblem>& tab, int bk, int fold_kb, int sm_count) {
+  for (GroupedProblem& p : tab) {
+    p.splits = 1;
+    p.kbs = 0;
+  }
+  if (tab.empty() || sm_count <= 0) return;
+  // GBBLAS_GROUPED_SPLITK: "0" never splits; N >= 2 cuts every problem of at
+  // least N k-blocks into N slices (tuning); unset or "1": the rule above
+  const char* env = std::getenv("GBBLAS_GROUPED_SPLITK");
+  const long forced = env ? std::strtol(env, nullptr, 10) : 1;
+  if (forced <= 0) return;
+  if (forced >= 2) {
+    for (GroupedProblem& p : tab) {
+      const int64_t nkp = p.k > 0 ? cdiv(p.k, bk) : 0;
+      if (nkp >= forced) slice_shape(nkp, cdiv(nkp, std::min<int64_t>(forced, kGtMaxSplits)), p.splits, p.kbs);
+      if (p.splits == 1) p.kbs = 0;
+    }
+    return;
+  }
+  const size_t np = tab.size();
+  std::vector<int64_t> out(np), nk(np), want(np, 1);
+  int64_t work = 0, nk_max = 0;
+  for (size_t i = 0; i < np; ++i) {
+    out[i] = cdiv(tab[i].m, kGtBM) * tab[i].tiles_n;
+    nk[i] = tab[i].k > 0 ? cdiv(tab[i].k, bk) : 0;
+    work += out[i] * nk[i];
+    nk_max = std::max(nk_max, nk[i]);
+  }
+  const int64_t min_kb = std::max<int64_t>(1, kGtMinSliceK / bk);
+  // nothing to gain unless the longest tile is well above the mean load
+  if (nk_max < 2 * min_kb || double(nk_max) <= 2.0 * double(work) / sm_count) return;
+  int64_t tiles = 0;
+  for (size_t i = 0; i < np; ++i) {
+    int64_t s = int64_t(std::sqrt(double(nk[i]) / fold_kb));
+    s = std::min<int64_t>({s, kGtMaxSplits, nk[i] / min_kb});
+    want[i] = std::max<int64_t>(1, s);
+    tiles += out[i] * want[i];
+  }
+  // one wave: halve the largest slice counts until the tiles fit
+  while (tiles > sm_count) {
+    int64_t smax = 1;
+    for (size_t i = 0; i < np; ++i) smax = std::max(smax, want[i]);
+    if (smax == 1) break;
+    for (size_t i = 0; i < np; ++i)
+      if (want[i] == smax) {
+        const int64_t h = std::max<int64_t>(1, smax / 2);
+        tiles -= out[i] * (smax - h);
+        want[i] = h;
+      }
+  }
+  for (size_t i = 0; i < np; ++i) {
+    if (want[i] > 1) slice_shape(nk[i], cdiv(nk[i], want[i]), tab[i].splits, tab[i].kbs);
+    if (tab[i].splits == 1) tab[i].kbs = 0;
+  }
+}
+
+// split_bk > 0: tcgen05 tiles with k-blocks of split_bk elements, split-K
+// planned for sm_count SMs (split_p BF16 term products per element).
 static gbblas_status_t build_table(int dtype, int64_t count, const char* transa, const char* transb,
                                    const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
                                    const void* const* a, const int64_t* lda, const void* const* b,
                                    const int64_t* ldb, const float* beta, float* const* c, const int64_t* ldc,
-                                   int tile_m, int tile_n, std::vector<GroupedProblem>& tab,
-                                   std::vector<int>& tile_prob, int64_t& tiles) {
+                                   int tile_m, int tile_n, int split_bk, int split_p, int sm_count,
+                                   std::vector<GroupedProblem>& tab, std::vector<int>& tile_prob, int64_t& tiles,
+                                   int64_t& part_floats, int64_t& n_ticks) {
   if (dtype != GBBLAS_DTYPE_F32 && dtype != GBBLAS_DTYPE_BF16)
     return fail(GBBLAS_STATUS_UNSUPPORTED, "grouped: element type must be F32 or BF16");
   if (count < 0 || count > (1 << 24)) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: bad problem count");
@@ -270,16 +368,37 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
     p.lda = lda[i];
     p.ldb = ldb[i];
     p.ldc = ldc[i];
+    p.splits = 1;
+    p.kbs = 0;
+    p.part_off = 0;
+    p.tick_off = 0;
+    p.src = i;
     tab.push_back(p);
   }
-  // longest tiles first; tiles numbered in that order
-  std::stable_sort(tab.begin(), tab.end(),
-                   [](const GroupedProblem& x, const GroupedProblem& y) { return x.k > y.k; });
+  if (split_bk > 0) {
+    // cost model per k-block: a BF16 k-block (one product) is ~3x shorter
+    // than an FP32 one (six products), so the fixed costs weigh more
+    plan_splits(tab, split_bk, split_p == 1 ? 4 : 3, sm_count);
+  }
+  // longest tiles (slices) first; tiles numbered in that order
+  auto tile_k = [](const GroupedProblem& p, int bk) { return p.splits > 1 ? int64_t(p.kbs) * bk : int64_t(p.k); };
+  std::stable_sort(tab.begin(), tab.end(), [&](const GroupedProblem& x, const GroupedProblem& y) {
+    return tile_k(x, split_bk) > tile_k(y, split_bk);
+  });
   tile_prob.clear();
+  part_floats = 0;
+  n_ticks = 0;
   for (size_t i = 0; i < tab.size(); ++i) {
     GroupedProblem& p = tab[i];
     p.tile_start = tiles;
-    const int64_t nt = cdiv(int64_t(p.m), tile_m) * p.tiles_n;
+    const int64_t out = cdiv(int64_t(p.m), tile_m) * p.tiles_n;
+    const int64_t nt = out * p.splits;
+    if (p.splits > 1) {
+      p.part_off = part_floats;
+      p.tick_off = n_ticks;
+      part_floats += out * p.splits * kGtTileFloats;
+      n_ticks += out * kGtSubs;
+    }
     tiles += nt;
     tile_prob.insert(tile_prob.end(), size_t(nt), int(i));
   }
@@ -402,11 +521,11 @@ static size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte layout of a launch's device block.
 struct GroupedLayout {
-  size_t table, tile_prob, counters, maps, ops, ctas, terms, total;
+  size_t table, tile_prob, counters, maps, ops, ctas, ticks, parts, terms, total;
 };
 
 static GroupedLayout grouped_layout(size_t count, size_t tiles, size_t n_maps, size_t n_ops, size_t n_ctas,
-                                    size_t term_bytes) {
+                                    size_t n_ticks, size_t part_floats, size_t term_bytes) {
   GroupedLayout L;
   L.table = 0;
   L.tile_prob = round256(sizeof(GroupedProblem) * std::max<size_t>(1, count));
@@ -414,7 +533,9 @@ static GroupedLayout grouped_layout(size_t count, size_t tiles, size_t n_maps, s
   L.maps = L.counters + 256;
   L.ops = L.maps + round256(sizeof(CUtensorMap) * n_maps);
   L.ctas = L.ops + round256(sizeof(GtOperand) * n_ops);
-  L.terms = L.ctas + round256(sizeof(int2) * n_ctas);
+  L.ticks = L.ctas + round256(sizeof(int2) * n_ctas);
+  L.parts = L.ticks + round256(sizeof(unsigned int) * n_ticks);
+  L.terms = L.parts + round256(sizeof(float) * part_floats);
   L.total = L.terms + term_bytes;
   return L;
 }
@@ -437,12 +558,17 @@ struct GroupedHost {
   std::vector<int2> ctas;
   size_t term_bytes = 0;
   int64_t tiles = 0;
+  int64_t part_floats = 0, n_ticks = 0;  // split-K
 };
+
+static GroupedLayout host_layout(const GroupedHost& H) {
+  return grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(),
+                        size_t(H.n_ticks), size_t(H.part_floats), H.term_bytes);
+}
 
 static GroupedLayout bind_plan(gbblas_handle_t h, int dtype, int method, GroupedHost& H, void* block,
                                gbblas_grouped_plan_s* pl) {
-  GroupedLayout L =
-      grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(), H.term_bytes);
+  GroupedLayout L = host_layout(H);
   uint8_t* b = static_cast<uint8_t*>(block);
   pl->dtype = dtype;
   pl->method = method;
@@ -457,19 +583,24 @@ static GroupedLayout bind_plan(gbblas_handle_t h, int dtype, int method, Grouped
   pl->n_ops = method == 1 ? int(H.ops.size()) : 0;
   pl->ctas = method == 1 ? reinterpret_cast<int2*>(b + L.ctas) : nullptr;
   pl->n_ctas = method == 1 ? int(H.ctas.size()) : 0;
+  pl->ticks = H.n_ticks > 0 ? reinterpret_cast<unsigned int*>(b + L.ticks) : nullptr;
+  pl->parts = H.part_floats > 0 ? reinterpret_cast<float*>(b + L.parts) : nullptr;
   return L;
 }
 
 // Host-side preparation shared by plans and one-shot calls.  The term area's
 // address is only known once the block exists, so the maps are encoded
 // against `block` (may be null while sizing).
-static gbblas_status_t prepare_host(int dtype, int method, int64_t count, const char* transa, const char* transb,
-                                    const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
-                                    const void* const* a, const int64_t* lda, const void* const* b,
-                                    const int64_t* ldb, const float* beta, float* const* c, const int64_t* ldc,
-                                    GroupedHost& H) {
+static gbblas_status_t prepare_host(gbblas_handle_t h, int dtype, int method, int64_t count, const char* transa,
+                                    const char* transb, const int64_t* m, const int64_t* n, const int64_t* k,
+                                    const float* alpha, const void* const* a, const int64_t* lda,
+                                    const void* const* b, const int64_t* ldb, const float* beta, float* const* c,
+                                    const int64_t* ldc, GroupedHost& H) {
+  const bool bf16 = dtype == GBBLAS_DTYPE_BF16;
+  const int split_bk = method == 1 ? (bf16 ? GtCfg<1>::BK : GtCfg<3>::BK) : 0;
   GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
-                     method ? kGtBM : kGT, method ? kGtBN : kGT, H.tab, H.tile_prob, H.tiles));
+                     method ? kGtBM : kGT, method ? kGtBN : kGT, split_bk, bf16 ? 1 : 3, h->sm_count, H.tab,
+                     H.tile_prob, H.tiles, H.part_floats, H.n_ticks));
   if (method == 1) {
     plan_tc_operands(dtype, H.tab, H.operands, H.term_bytes);
     // sizes only: maps two per problem, one conversion per non-direct operand
@@ -494,6 +625,7 @@ static gbblas_status_t upload(const GroupedHost& H, const GroupedLayout& L, uint
     GB_CUDA_TRY(cudaMemcpyAsync(block + L.tile_prob, H.tile_prob.data(), sizeof(int) * H.tile_prob.size(),
                                 cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemsetAsync(block + L.counters, 0, 2 * sizeof(unsigned long long), s));
+  if (H.n_ticks > 0) GB_CUDA_TRY(cudaMemsetAsync(block + L.ticks, 0, sizeof(unsigned int) * size_t(H.n_ticks), s));
   if (!H.maps.empty() && L.ops > L.maps)
     GB_CUDA_TRY(cudaMemcpyAsync(block + L.maps, H.maps.data(), sizeof(CUtensorMap) * H.maps.size(),
                                 cudaMemcpyHostToDevice, s));
@@ -520,13 +652,12 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
   *out = nullptr;
   const int method = grouped_method();
   GroupedHost H;
-  GB_TRY(prepare_host(dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
+  GB_TRY(prepare_host(h, dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
   auto* plan = new (std::nothrow) gbblas_grouped_plan_s();
   if (!plan) return fail(GBBLAS_STATUS_ALLOC_FAILED, "grouped: out of host memory");
   plan->err = h->dev_error;
   plan->device = h->device;
-  const GroupedLayout L0 =
-      grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(), H.term_bytes);
+  const GroupedLayout L0 = host_layout(H);
   cudaError_t e = cudaMalloc(&plan->block, L0.total);
   if (e != cudaSuccess) {
     delete plan;
@@ -546,7 +677,43 @@ gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t
     gbblas_grouped_plan_destroy(plan);
     return st;
   }
+  for (const GroupedProblem& p : H.tab) plan->max_splits = std::max(plan->max_splits, p.splits);
   *out = plan;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status_t gbblas_grouped_schedule(int dtype, int64_t count, const char* transa, const char* transb,
+                                        const int64_t* m, const int64_t* n, const int64_t* k, const float* alpha,
+                                        int sm_count, int64_t* tiles, int* splits) {
+  clear_error();
+  if (sm_count < 1) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped schedule: sm_count < 1");
+  if (count < 0 || count > (1 << 24)) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: bad problem count");
+  // the planner only looks at sizes: stand-in operands and scalars
+  std::vector<const void*> ptr(size_t(count), reinterpret_cast<const void*>(uintptr_t(256)));
+  std::vector<float*> cptr(size_t(count), reinterpret_cast<float*>(uintptr_t(256)));
+  std::vector<float> zero(size_t(count), 0.f);
+  std::vector<int64_t> ld(size_t(count), 1);
+  for (int64_t i = 0; i < count && m && n && k; ++i) ld[size_t(i)] = std::max<int64_t>({1, m[i], n[i], k[i]});
+  const bool bf16 = dtype == GBBLAS_DTYPE_BF16;
+  std::vector<GroupedProblem> tab;
+  std::vector<int> tile_prob;
+  int64_t n_tiles = 0, part_floats = 0, n_ticks = 0;
+  GB_TRY(build_table(dtype, count, transa, transb, m, n, k, alpha, ptr.data(), ld.data(), ptr.data(), ld.data(),
+                     zero.data(), cptr.data(), ld.data(), kGtBM, kGtBN, bf16 ? GtCfg<1>::BK : GtCfg<3>::BK,
+                     bf16 ? 1 : 3, sm_count, tab, tile_prob, n_tiles, part_floats, n_ticks));
+  if (tiles) *tiles = n_tiles;
+  if (splits) {
+    for (int64_t i = 0; i < count; ++i) splits[i] = 0;  // empty problems (m or n == 0) have no tiles
+    for (const GroupedProblem& p : tab) splits[p.src] = p.splits;
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status_t gbblas_grouped_plan_info(gbblas_grouped_plan_t plan, int64_t* tiles, int* max_splits) {
+  clear_error();
+  if (!plan) return fail(GBBLAS_STATUS_INVALID_ARG, "grouped: null plan");
+  if (tiles) *tiles = plan->total_tiles;
+  if (max_splits) *max_splits = plan->max_splits;
   return GBBLAS_STATUS_SUCCESS;
 }
 
@@ -590,11 +757,10 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
   if (!h) return fail(GBBLAS_STATUS_NOT_INITIALIZED, "grouped: null handle");
   const int method = grouped_method();
   GroupedHost H;
-  GB_TRY(prepare_host(dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
+  GB_TRY(prepare_host(h, dtype, method, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, H));
   if (H.tiles == 0) return GBBLAS_STATUS_SUCCESS;
   // one-shot: the whole block lives in the handle's stream-ordered temp memory
-  const GroupedLayout L0 =
-      grouped_layout(H.tab.size(), size_t(H.tiles), H.maps.size(), H.ops.size(), H.ctas.size(), H.term_bytes);
+  const GroupedLayout L0 = host_layout(H);
   void* ws = nullptr;
   GB_TRY(temp_acquire(h, L0.total, &ws));
   gbblas_grouped_plan_s tmp;

@@ -293,13 +293,30 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
   }
 }
 
+// Split-K: a problem whose tiles are much longer (in K) than the average work
+// per SM is cut into `splits` K slices per output tile; its tiles are
+// numbered slice-major (tile = slice * output tiles + output tile).  Each
+// epilogue warp owns a 32-row x 64-column sub-block of the output tile; it
+// writes its slice's FP32 partial sub-block (column-major, 32 lanes per
+// column, so the stores coalesce) and takes the sub-block's ticket.  The warp
+// that takes the last ticket adds the slices in index order (deterministic,
+// whatever the arrival order), applies alpha / beta, stores C and resets the
+// ticket, so a graph can replay the launch.  No barrier spans warps.
+constexpr int kGtSubs = 8;                  // epilogue sub-blocks per output tile
+constexpr int kGtSubFloats = 32 * 64;       // floats per sub-block
+constexpr int kGtTileFloats = kGtSubs * kGtSubFloats;
+
 // One scheduled tile (prob < 0: no more tiles).
 struct GtWork {
-  int prob, nk, m0, n0;  // problem, k-blocks, tile origin
+  int prob, nk, m0, n0;  // problem, k-blocks of this slice, tile origin
   int m, n;              // the problem's C extent
+  int kb0;               // first k-block of this slice
+  int slice, splits;     // K slice of the output tile, and their number
   float alpha, beta;
   float* c;
   int64_t ldc;
+  float* part;           // split-K: slice 0's partial block of this output tile
+  unsigned int* tick;    // split-K: the output tile's kGtSubs tickets
 };
 
 // tiles the scheduler takes from the counter at a time
@@ -316,12 +333,15 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
 // down groups of kGtGroupM tile rows, then along N); tile_prob[t]: problem
 // of tile t; maps[2p], maps[2p+1]: tensor maps of problem p's A terms ([P][m][Kp]) and B terms
 // ([P][n][Kp]), box 64 x rows x P; counters[0] = next tile, counters[1] =
-// CTAs finished (the last one resets both, so a graph can replay the launch).
+// CTAs finished (the last one resets both, so a graph can replay the launch);
+// parts / ticks: split-K partial blocks and tickets (problem fields
+// part_off / tick_off index them).
 template <int P, int CHUNK, class Prob>
 __global__ void __launch_bounds__(kGtThreads, 1)
     grouped_tc_kernel(const Prob* __restrict__ probs, const int* __restrict__ tile_prob,
                       const CUtensorMap* __restrict__ maps, int64_t total_tiles,
-                      unsigned long long* __restrict__ counters, int* __restrict__ err) {
+                      unsigned long long* __restrict__ counters, float* __restrict__ parts,
+                      unsigned int* __restrict__ ticks, int* __restrict__ err) {
   using Cfg = GtCfg<P>;
   constexpr int S = Cfg::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -367,7 +387,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
     // CTAs finish together
     __shared__ GtWork batch[kGtBatch];
     uint32_t i = 0;
-    int take = kGtBatch;
+    int take = 2ll * kGtBatch * gridDim.x >= total_tiles ? 1 : kGtBatch;
     bool more = true;
     while (more) {
       long long base = 0;
@@ -380,12 +400,25 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         if (tile < total_tiles) {
           const int p = __ldg(tile_prob + tile);
           const Prob& pr = probs[p];
-          const int local = int(tile - pr.tile_start);
+          int local = int(tile - pr.tile_start);
+          const int tiles_m = (pr.m + kGtBM - 1) / kGtBM;
+          const int nk_all = pr.k > 0 ? (pr.k + Cfg::BK - 1) / Cfg::BK : 0;
           w.prob = p;
-          w.nk = pr.k > 0 ? (pr.k + Cfg::BK - 1) / Cfg::BK : 0;
+          w.splits = pr.splits;
+          w.slice = 0;
+          w.kb0 = 0;
+          w.nk = nk_all;
+          if (pr.splits > 1) {
+            const int out_tiles = tiles_m * pr.tiles_n;
+            w.slice = local / out_tiles;
+            local -= w.slice * out_tiles;
+            w.kb0 = w.slice * pr.kbs;
+            w.nk = min(pr.kbs, nk_all - w.kb0);
+            w.part = parts + pr.part_off + int64_t(local) * pr.splits * kGtTileFloats;
+            w.tick = ticks + pr.tick_off + int64_t(local) * kGtSubs;
+          }
           // tiles of a problem go down kGtGroupM M tiles, then along N, so the
           // CTAs working at the same time share A and B panels in L2
-          const int tiles_m = (pr.m + kGtBM - 1) / kGtBM;
           const int per_group = kGtGroupM * pr.tiles_n;
           const int first_m = (local / per_group) * kGtGroupM, in = local % per_group;
           const int gsize = min(tiles_m - first_m, kGtGroupM);
@@ -457,8 +490,8 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           }
           tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
           uint8_t* st = smem + s * Cfg::STAGE;
-          tc::tma_load_3d(st, ma, &full[s], kb * Cfg::BK, w.m0, 0);
-          tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kb * Cfg::BK, w.n0, 0);
+          tc::tma_load_3d(st, ma, &full[s], (w.kb0 + kb) * Cfg::BK, w.m0, 0);
+          tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], (w.kb0 + kb) * Cfg::BK, w.n0, 0);
         }
         if (!ok) break;
       }
@@ -564,6 +597,27 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         if (lane == 0) tc::mbar_arrive(&tempty[b]);
       }
       if (!ok) break;
+      if (w.splits > 1) {
+        const int sub = h * 4 + q;
+        float* mine = w.part + (int64_t(w.slice) * kGtSubs + sub) * kGtSubFloats + lane;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) __stcg(mine + j * 32, sum[j]);
+        __threadfence();
+        __syncwarp();
+        unsigned last = 0;
+        if (lane == 0) last = atomicAdd(w.tick + sub, 1u) == unsigned(w.splits - 1) ? 1u : 0u;
+        if (__shfl_sync(0xffffffffu, last, 0) == 0u) continue;
+        __threadfence();
+        const float* src = w.part + int64_t(sub) * kGtSubFloats + lane;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) sum[j] = __ldcg(src + j * 32);
+        for (int sl = 1; sl < w.splits; ++sl) {
+          src += int64_t(kGtSubs) * kGtSubFloats;
+#pragma unroll
+          for (int j = 0; j < 64; ++j) sum[j] += __ldcg(src + j * 32);
+        }
+        if (lane == 0) w.tick[sub] = 0u;
+      }
       const int64_t gm = int64_t(w.m0) + q * 32 + lane;
       if (gm < w.m) {
         float* const c = w.c;

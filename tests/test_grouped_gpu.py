@@ -173,3 +173,64 @@ def test_grouped_large_problems_tile_grouping(sb, torch_cuda, dtype, method):
         got = p["c"].cpu().numpy().reshape(n, ldc).T[rows, cols]
         np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * max(1, k))
     sb.check_device_error()
+
+
+@pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
+@pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
+def test_grouped_split_k_long_k(sb, torch_cuda, dtype, method):
+    """A few long-K problems beside a small one: the plan cuts their K into
+    slices (split-K, tall-skinny); the FP32 partials of the slices are added
+    in slice order by whichever CTA finishes last, so two runs agree bit for
+    bit, and beta is applied once.  Sampled entries against the oracle,
+    normalised by |alpha| |A||B| + |beta C|."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(71)
+    shapes = [(48, 48, 1 << 17, False, False), (200, 130, 20000, True, False), (130, 300, 9001, False, True),
+              (1, 1, 70000, True, True), (20, 30, 40, False, False)]
+    probs, host = [], []
+    for (m, n, k, ta, tb) in shapes:
+        lda, ldb, ldc = (k if ta else m) + 1, (n if tb else k) + 2, m + 3
+        a = g.uniform(-1, 1, lda * (m if ta else k)).astype(np.float32)
+        b = g.uniform(-1, 1, ldb * (k if tb else n)).astype(np.float32)
+        c = g.uniform(-1, 1, ldc * n).astype(np.float32)
+        if dtype == "bfloat16":
+            a = torch.from_numpy(a).bfloat16().float().numpy()
+            b = torch.from_numpy(b).bfloat16().float().numpy()
+        tdt = torch.bfloat16 if dtype == "bfloat16" else torch.float32
+        probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=m, n=n, k=k, alpha=1.5,
+                          a=torch.from_numpy(a).to(tdt).cuda(), lda=lda, b=torch.from_numpy(b).to(tdt).cuda(),
+                          ldb=ldb, beta=0.5, c=torch.from_numpy(c).cuda(), ldc=ldc))
+        host.append((ta, tb, m, n, k, a, lda, b, ldb, c, ldc))
+    c0 = [p["c"].clone() for p in probs]
+    plan = blas.GroupedPlan(sb, probs, dtype=dtype)
+    tiles, splits = plan.info()
+    assert splits > 1 and tiles > 8
+    plan.run()
+    sb.wait()
+    first = [p["c"].clone() for p in probs]
+    for p, (ta, tb, m, n, k, a, lda, b, ldb, c, ldc) in zip(probs, host):
+        rows = g.integers(0, m, 48)
+        cols = g.integers(0, n, 48)
+        ref = oracle.gemm(ta, tb, m, n, k, 1.5, a, lda, b, ldb, 0.5, c, ldc, rows=rows, cols=cols)
+        scale = oracle.gemm_absscale(ta, tb, m, n, k, 1.5, a, lda, b, ldb, 0.5, c, ldc, rows=rows, cols=cols)
+        got = p["c"].cpu().numpy().reshape(n, ldc).T[rows, cols]
+        assert (np.abs(got - ref) / scale).max() <= 1e-5, (m, n, k)
+    for p, c in zip(probs, c0):
+        p["c"].copy_(c)
+    plan.run()
+    sb.wait()
+    for p, f in zip(probs, first):
+        assert torch.equal(p["c"], f)
+    plan.close()
+    sb.check_device_error()
+
+
+@pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
+def test_grouped_no_split_for_many_short_problems(sb, torch_cuda, method):
+    """Many short problems (no tile dominates the load): no K is split."""
+    from portblas_gb300 import blas
+    probs, _ = _problems(torch_cuda, rng(73), 200, 16, 400, "float32")
+    plan = blas.GroupedPlan(sb, probs, dtype="float32")
+    assert plan.info()[1] == 1
+    plan.close()
