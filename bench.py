@@ -143,9 +143,9 @@ def make_inputs(torch, dev):
     return dict(A=A, xg=xg, v=v, w=w, R=R, planted=int(idx.min().item()))
 
 
-def run_step(blas, sb, inp, outs, events=None):
-    """One pass of the memory-bound set; `events` (optional) brackets each op."""
-    ops = [
+def step_ops(blas, sb, inp, outs):
+    """The memory-bound set as (name, call) pairs, in step order."""
+    return [
         ("gemv_n", lambda: blas._gemv(sb, "n", GEMV_N, GEMV_N, 1.0, inp["A"], GEMV_N, inp["xg"], 1, 0.0,
                                       outs["yn"], 1)),
         ("gemv_t", lambda: blas._gemv(sb, "t", GEMV_N, GEMV_N, 1.0, inp["A"], GEMV_N, inp["xg"], 1, 0.0,
@@ -160,6 +160,11 @@ def run_step(blas, sb, inp, outs, events=None):
         ("reduction_outer", lambda: blas.extension._reduction(blas.AddOperator, sb, inp["R"], RED_N, outs["ro"],
                                                               RED_N, RED_N, blas.reduction_dim_t.outer)),
     ]
+
+
+def run_step(blas, sb, inp, outs, events=None):
+    """One pass of the memory-bound set; `events` (optional) brackets each op."""
+    ops = step_ops(blas, sb, inp, outs)
     for i, (name, fn) in enumerate(ops):
         ev = events.get(name) if events is not None else None
         if ev is not None:
@@ -191,6 +196,27 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev, record_ops=True):
         for n in names:
             per_op[n].append(ev[n][0].elapsed_time(ev[n][1]))
     dom = max(names, key=lambda n: statistics.median(per_op[n])) if record_ops else None
+    # per-op time in a pipeline: PIPE back-to-back calls of one op between two
+    # events (the event and launch cost of a lone call, ~4 us, is then spread
+    # over the calls).  Consecutive calls alternate between two copies of the
+    # inputs, so no call finds its operands in L2; median of three runs
+    PIPE = 8
+    per_op_pipe = {n: [] for n in names}
+    if record_ops:
+        inp2 = {k: (v.clone() if hasattr(v, "clone") else v) for k, v in inp.items()}
+        pairs = zip(step_ops(blas, sb, inp, outs), step_ops(blas, sb, inp2, outs))
+        for (name, fn), (_, fn2) in pairs:
+            fn()
+            fn2()
+            for _ in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for c in range(PIPE):
+                    (fn2 if c & 1 else fn)()
+                e1.record()
+                torch.cuda.synchronize()
+                per_op_pipe[name].append(e0.elapsed_time(e1) / PIPE)
+        del inp2, pairs
     # the timed region: K whole steps between two events, enqueued back to
     # back; inside it, two events on the same stream bracket the dominant op
     # of every step (events around all nine ops would slow the step by ~6%)
@@ -217,6 +243,7 @@ def bench_memory_set(torch, blas, sb, steps, warmup, dev, record_ops=True):
     iam = outs["i"].cpu().numpy()
     checks = {"iamax_index": int(iam[0]), "iamax_expected_first_planted": inp["planted"]}
     return dict(ms=ms, per_op={n: statistics.median(v) if v else None for n, v in per_op.items()},
+                per_op_pipe={n: statistics.median(v) if v else None for n, v in per_op_pipe.items()},
                 dom=dom, dom_ms=dom_ms, launches=launches, errors=fp64_errors(torch, inp, outs),
                 clocks=clk.summary(), checks=checks, inp=inp, outs=outs)
 
@@ -728,9 +755,12 @@ def main():
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)", "config": config,
         "hbm_frac_of_" + pk["src"]: value / world / pk["hbm_gbs"],
-        "per_op": {n: {"ms": t, "gbs": ab[n] / (t * 1e-3) / 1e9, "frac": ab[n] / (t * 1e-3) / 1e9 / pk["hbm_gbs"],
+        # per op: "ms" / "gbs" / "frac" from 8 back-to-back calls between two
+        # events; "*_single_call" from one call between two events
+        "per_op": {n: {"ms": tp, "gbs": ab[n] / (tp * 1e-3) / 1e9, "frac": ab[n] / (tp * 1e-3) / 1e9 / pk["hbm_gbs"],
+                       "ms_single_call": t, "frac_single_call": ab[n] / (t * 1e-3) / 1e9 / pk["hbm_gbs"],
                        "rel_err_vs_fp64": mem["errors"].get(n)}
-                   for n, t in mem["per_op"].items()},
+                   for n, t in mem["per_op"].items() for tp in [mem["per_op_pipe"][n]]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "peak_src": pk["src"],
                      "traffic": NCU_TRAFFIC.get(dom), "traffic_unit": "bytes per launch (ncu)",
