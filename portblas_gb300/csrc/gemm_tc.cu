@@ -41,22 +41,27 @@ struct TcCfg {
   static constexpr int B_TILE = BN * kTcBK * 2;
   static constexpr int STAGE = P * (A_TILE + B_TILE);
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
-  static constexpr int NPAIRS = P == 1 ? 1 : (P == 2 ? 3 : 6);
-  static constexpr int TMEM_COLS = 2 * BN;  // two chunk accumulators
+  static constexpr int NPAIRS = P == 1 ? 1 : 3;  // term products issued one by one (P <= 2)
+  // columns of one chunk accumulator: with P = 3 the products of an A term
+  // with the two adjacent leading B terms are one N = 2*BN MMA, and the
+  // epilogue adds the two column halves
+  static constexpr int ACC = P == 3 ? 2 * BN : BN;
+  static constexpr int TMEM_COLS = 2 * ACC;  // two chunk accumulators
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
   static_assert(TMEM_COLS <= 512, "tensor memory budget");
 };
+
+// term pairs (a-term, b-term) of the P <= 2 splits, largest first:
+// P = 1: (0,0); P = 2: (0,0) (0,1) (1,0)
+__device__ __forceinline__ void term_pair(int q, int& pa, int& pb) {
+  pa = q == 2 ? 1 : 0;
+  pb = q == 1 ? 1 : 0;
+}
 
 // k-blocks (of 64) accumulated in tensor memory before the partial sum is
 // promoted into the FP32 register accumulator of the epilogue warps
 constexpr int kTcChunk = 4;
 
-// term pairs (a-term, b-term) with a + b <= P - 1, largest first:
-// P = 1: (0,0); P = 2: (0,0) (0,1) (1,0); P = 3: + (0,2) (1,1) (2,0)
-__device__ __forceinline__ void term_pair(int q, int& pa, int& pb) {
-  pa = (q == 2 || q == 4) ? 1 : (q == 5 ? 2 : 0);
-  pb = (q == 1 || q == 4) ? 1 : (q == 3 ? 2 : 0);
-}
 
 enum : int { kErrTcProducer = 101, kErrTcMma = 102, kErrTcEpilogue = 103, kErrTcDrain = 104 };
 
@@ -146,6 +151,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, BN);
+      constexpr uint32_t idesc2 = tc::idesc_bf16_f32(kTcBM, 2 * BN);
       bool ok = true;
       for (int c = 0; c < nchunks && ok; ++c) {
         const int b = c & 1;
@@ -155,7 +161,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           break;
         }
         tc::tc_fence_after();
-        const uint32_t acc = tmem + uint32_t(b * BN);
+        const uint32_t acc = tmem + uint32_t(b * Cfg::ACC);
         const int kb1 = min(nk, (c + 1) * kTcChunk);
         for (int kb = c * kTcChunk; kb < kb1; ++kb) {
           const int s = kb % STAGES;
@@ -167,15 +173,36 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           tc::tc_fence_after();
           const uint8_t* st = tiles + s * Cfg::STAGE;
+          if constexpr (P <= 2) {
 #pragma unroll
-          for (int q = 0; q < Cfg::NPAIRS; ++q) {
-            int pa, pb;
-            term_pair(q, pa, pb);
-            const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
-            const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+            for (int q = 0; q < Cfg::NPAIRS; ++q) {
+              int pa, pb;
+              term_pair(q, pa, pb);
+              const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+              const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
 #pragma unroll
-            for (int j = 0; j < kTcBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
-              tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+              for (int j = 0; j < kTcBK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
+                tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+            }
+          } else {
+            // P = 3: the B terms are adjacent BN-row tiles, so B terms (0, 1)
+            // form one 2*BN-row operand.  a(0) x [b0; b1] fills both column
+            // halves (the first MMA of a chunk initialises both), a(1) x
+            // [b0; b1] adds to both, a(0) b(2) and a(2) b(0) go to the second
+            // half: the six products of the split, the leading one kept apart
+            // from the small cross terms.
+            const uint32_t sa = tc::smem_u32(st), sb = tc::smem_u32(st + P * Cfg::A_TILE);
+            const uint64_t a0 = tc::sdesc_kmajor_sw128(sa), a1 = tc::sdesc_kmajor_sw128(sa + Cfg::A_TILE);
+            const uint64_t a2 = tc::sdesc_kmajor_sw128(sa + 2 * Cfg::A_TILE);
+            const uint64_t b01 = tc::sdesc_kmajor_sw128(sb), b2 = tc::sdesc_kmajor_sw128(sb + 2 * Cfg::B_TILE);
+            const uint32_t acc2 = acc + uint32_t(BN);
+#pragma unroll
+            for (int j = 0; j < kTcBK / 16; ++j) {  // K = 16 per MMA: +32 bytes in the swizzled row
+              tc::mma_bf16(acc, a0 + 2 * j, b01 + 2 * j, idesc2, (kb != c * kTcChunk) || j != 0);
+              tc::mma_bf16(acc, a1 + 2 * j, b01 + 2 * j, idesc2, true);
+              tc::mma_bf16(acc2, a0 + 2 * j, b2 + 2 * j, idesc, true);
+              tc::mma_bf16(acc2, a2 + 2 * j, b01 + 2 * j, idesc, true);
+            }
           }
           tc::mma_commit(&empty[s]);
         }
@@ -201,12 +228,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       tc::tc_fence_after();
 #pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = 0; c0 < Cfg::ACC; c0 += 32) {  // column halves fold onto the same BN sums
         uint32_t r[32];
-        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * BN + c0), r);
+        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * Cfg::ACC + c0), r);
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int i = 0; i < 32; ++i) sum[c0 + i] += __uint_as_float(r[i]);
+        for (int i = 0; i < 32; ++i) sum[(c0 + i) % BN] += __uint_as_float(r[i]);
       }
       tc::tc_fence_before();
       __syncwarp();
