@@ -64,8 +64,13 @@ struct GtCfg {
   // barriers: full/empty per stage, two accumulator pairs, a work-slot pair per ring entry; then the TMEM address
   static constexpr int BARRIER_BYTES = (2 * STAGES + 2 * kGtAcc + 2 * kGtRing) * 8 + 4;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
-  static constexpr int NPAIRS = P == 1 ? 1 : (P == 2 ? 3 : 6);
-  static constexpr int TMEM_COLS = kGtAcc * kGtBN;  // the chunk accumulators
+  static constexpr int NPAIRS = P == 1 ? 1 : 3;  // term products issued one by one (P <= 2)
+  // columns of one chunk accumulator: with P = 3 the products of an A term
+  // with the two adjacent leading B terms are one N = 256 MMA, and the
+  // epilogue adds the two column halves
+  static constexpr int ACC = P == 3 ? 2 * kGtBN : kGtBN;
+  static constexpr int TMEM_COLS = kGtAcc * ACC;  // the chunk accumulators
+  static_assert(TMEM_COLS <= 512, "tensor memory budget");
   static_assert(BARRIER_BYTES <= 512, "barrier area");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
@@ -506,6 +511,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
     // ---------------------------------------------------------- MMA issuer --
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_bf16_f32(kGtBM, kGtBN);
+      constexpr uint32_t idesc2 = tc::idesc_bf16_f32(kGtBM, 2 * kGtBN);
       uint32_t it = 0, g = 0;
       bool ok = true;
       for (uint32_t i = 0; ok; ++i) {
@@ -526,7 +532,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
             break;
           }
           tc::tc_fence_after();
-          const uint32_t acc = tmem + uint32_t(b * kGtBN);
+          const uint32_t acc = tmem + uint32_t(b * Cfg::ACC);
           const int kb1 = min(w.nk, (c + 1) * CHUNK);
           for (int kb = c * CHUNK; kb < kb1; ++kb, ++it) {
             const int s = it % S;
@@ -537,17 +543,37 @@ __global__ void __launch_bounds__(kGtThreads, 1)
             }
             tc::tc_fence_after();
             const uint8_t* st = smem + s * Cfg::STAGE;
+            auto desc = [](uint32_t a) {
+              return Cfg::BK == 64 ? tc::sdesc_kmajor_sw128(a) : tc::sdesc_kmajor_sw64(a);
+            };
+            if constexpr (P <= 2) {
 #pragma unroll
-            for (int q = 0; q < Cfg::NPAIRS; ++q) {
-              const int pa = (q == 2 || q == 4) ? 1 : (q == 5 ? 2 : 0);
-              const int pb = (q == 1 || q == 4) ? 1 : (q == 3 ? 2 : 0);
-              const uint32_t sa = tc::smem_u32(st + pa * Cfg::A_TILE);
-              const uint32_t sbb = tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE);
-              const uint64_t ad = Cfg::BK == 64 ? tc::sdesc_kmajor_sw128(sa) : tc::sdesc_kmajor_sw64(sa);
-              const uint64_t bd = Cfg::BK == 64 ? tc::sdesc_kmajor_sw128(sbb) : tc::sdesc_kmajor_sw64(sbb);
+              for (int q = 0; q < Cfg::NPAIRS; ++q) {  // (0,0) (0,1) (1,0)
+                const int pa = q == 2 ? 1 : 0, pb = q == 1 ? 1 : 0;
+                const uint64_t ad = desc(tc::smem_u32(st + pa * Cfg::A_TILE));
+                const uint64_t bd = desc(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
 #pragma unroll
-              for (int j = 0; j < Cfg::BK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
-                tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, kb != c * CHUNK || q != 0 || j != 0);
+                for (int j = 0; j < Cfg::BK / 16; ++j)  // K = 16 per MMA: +32 bytes in the swizzled row
+                  tc::mma_bf16(acc, ad + 2 * j, bd + 2 * j, idesc, kb != c * CHUNK || q != 0 || j != 0);
+              }
+            } else {
+              // P = 3: the B terms are adjacent 128-row tiles, so B terms
+              // (0, 1) form one 256-row operand.  a(0) x [b0; b1] fills both
+              // column halves (the first MMA of a chunk initialises both),
+              // a(1) x [b0; b1] adds to both, a(0) b(2) and a(2) b(0) go to the
+              // second half: the six products in four MMAs, the leading ones
+              // kept apart from the small cross terms.
+              const uint32_t sa = tc::smem_u32(st), sb = tc::smem_u32(st + P * Cfg::A_TILE);
+              const uint64_t a0 = desc(sa), a1 = desc(sa + Cfg::A_TILE), a2 = desc(sa + 2 * Cfg::A_TILE);
+              const uint64_t b01 = desc(sb), b2 = desc(sb + 2 * Cfg::B_TILE);
+              const uint32_t acc2 = acc + uint32_t(kGtBN);
+#pragma unroll
+              for (int j = 0; j < Cfg::BK / 16; ++j) {  // K = 16 per MMA: +32 bytes in the swizzled row
+                tc::mma_bf16(acc, a0 + 2 * j, b01 + 2 * j, idesc2, kb != c * CHUNK || j != 0);
+                tc::mma_bf16(acc, a1 + 2 * j, b01 + 2 * j, idesc2, true);
+                tc::mma_bf16(acc2, a0 + 2 * j, b2 + 2 * j, idesc, true);
+                tc::mma_bf16(acc2, a2 + 2 * j, b01 + 2 * j, idesc, true);
+              }
             }
             tc::mma_commit(&empty[s]);
           }
@@ -585,13 +611,16 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         }
         tc::tc_fence_after();
 #pragma unroll
-        for (int c0 = 0; c0 < 64; c0 += 32) {
-          uint32_t v[32];
-          tc::tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kGtBN + h * 64 + c0), v);
-          tc::tmem_ld_wait();
+        for (int part = 0; part < Cfg::ACC / kGtBN; ++part)  // column halves fold onto the same sums
 #pragma unroll
-          for (int j = 0; j < 32; ++j) sum[c0 + j] += __uint_as_float(v[j]);
-        }
+          for (int c0 = 0; c0 < 64; c0 += 32) {
+            uint32_t v[32];
+            tc::tmem_ld_32x32b_x32(
+                tmem + (uint32_t(q * 32) << 16) + uint32_t(b * Cfg::ACC + part * kGtBN + h * 64 + c0), v);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) sum[c0 + j] += __uint_as_float(v[j]);
+          }
         tc::tc_fence_before();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&tempty[b]);
