@@ -205,9 +205,10 @@ def test_dgemm_strided_batched(sb, torch_cuda):
 
 @pytest.mark.parametrize("ta", [False, True])
 def test_split_bf16x6_is_fp32_accurate(sb, torch_cuda, ta):
-    """The 3-term split with chunked tensor-memory accumulation matches the
-    accuracy of plain FP32 on wide-range data (entries s*2^u, u ~ U[-10, 10])
-    at K = 4096, measured against the FP64 oracle."""
+    """The 3-term split with chunked tensor-memory accumulation, its leading
+    products kept in their own accumulator, is at least as accurate as plain
+    FP32 on wide-range data (entries s*2^u, u ~ U[-10, 10]) at K = 4096,
+    measured against the FP64 oracle."""
     torch = torch_cuda
     from portblas_gb300 import blas
     g = rng(41)
@@ -228,8 +229,8 @@ def test_split_bf16x6_is_fp32_accurate(sb, torch_cuda, ta):
         errs[mode] = (float(e.mean()), float(e.max()))
     simt_mean, simt_max = errs["fp32_simt"]
     x6_mean, x6_max = errs["split_bf16x6"]
-    assert x6_mean <= 2.0 * simt_mean + 1e-9, errs
-    assert x6_max <= 4.0 * simt_max + 1e-8, errs
+    assert x6_mean <= simt_mean, errs
+    assert x6_max <= simt_max, errs
     assert errs["split_bf16x3"][1] <= 6e-5, errs  # the dropped 2^-16 terms bound the 2-term split
 
 
