@@ -284,6 +284,13 @@ class CBlas:
         L.scipy_cblas_sdot64_.restype = f32
         L.scipy_cblas_isamax64_.argtypes = [i64, P, i64]
         L.scipy_cblas_isamax64_.restype = i64
+        L.scipy_cblas_saxpy64_.argtypes = [i64, f32, P, i64, P, i64]
+        L.scipy_cblas_sscal64_.argtypes = [i64, f32, P, i64]
+        L.scipy_cblas_scopy64_.argtypes = [i64, P, i64, P, i64]
+        L.scipy_cblas_sdsdot64_.argtypes = [i64, f32, P, i64, P, i64]
+        L.scipy_cblas_sdsdot64_.restype = f32
+        L.scipy_cblas_ssymm64_.argtypes = [i32, i32, i32, i64, i64, f32, P, i64, P, i64, f32, P, i64]
+        L.scipy_cblas_somatcopy64_.argtypes = [i32, i32, i64, i64, f32, P, i64, P, i64]
         for nm in ("scipy_openblas_set_num_threads64_", "scipy_openblas_get_num_threads64_"):
             if not hasattr(L, nm):
                 raise OSError(f"{nm} missing from {self.path}")
@@ -322,6 +329,30 @@ class CBlas:
 
     def isamax(self, n, x, incx):
         return int(self.L.scipy_cblas_isamax64_(n, _p(x), incx))
+
+    def saxpy(self, n, alpha, x, incx, y, incy):
+        self.L.scipy_cblas_saxpy64_(n, alpha, _p(x), incx, _p(y), incy)
+
+    def sscal(self, n, alpha, x, incx):
+        self.L.scipy_cblas_sscal64_(n, alpha, _p(x), incx)
+
+    def scopy(self, n, x, incx, y, incy):
+        self.L.scipy_cblas_scopy64_(n, _p(x), incx, _p(y), incy)
+
+    def sdsdot(self, n, sb, x, incx, y, incy):
+        return self.L.scipy_cblas_sdsdot64_(n, sb, _p(x), incx, _p(y), incy)
+
+    Left, Right, Upper, Lower = 141, 142, 121, 122
+
+    def ssymm(self, side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc):
+        sd = self.Left if side in ("l", "L") else self.Right
+        ul = self.Upper if uplo in ("u", "U") else self.Lower
+        self.L.scipy_cblas_ssymm64_(self.ColMajor, sd, ul, m, n, alpha, _p(a), lda, _p(b), ldb, beta, _p(c), ldc)
+
+    def somatcopy(self, trans, m, n, alpha, a, lda, b, ldb):
+        """OpenBLAS extension: b <- alpha * op(a), a is m x n (column-major)."""
+        t = self.NoTrans if trans in ("n", "N") else self.Trans
+        self.L.scipy_cblas_somatcopy64_(self.ColMajor, t, m, n, alpha, _p(a), lda, _p(b), ldb)
 
     @staticmethod
     def isamin(n, x, incx):

@@ -162,3 +162,68 @@ def test_oracle_reduction_vs_numpy(op, dim):
            "abs_add": np.abs(mat).sum(axis), "mean": mat.mean(axis)}[op]
     got = oracle.reduction(op, dim, full, ld, rows, cols)
     np.testing.assert_allclose(got, ref, rtol=1e-12)
+
+
+@pytest.mark.parametrize("incx,incy", [(1, 1), (2, 3), (3, -2)])
+def test_oracle_axpy_copy_vs_cblas(cblas, incx, incy):
+    """_axpy and _copy restatements against CBLAS on strided views (negative
+    increments walk the vector from its end, as in portBLAS's VectorView)."""
+    g = rng(5)
+    n = 1001
+    x = g.standard_normal(n * abs(incx)).astype(np.float32)
+    y = g.standard_normal(n * abs(incy)).astype(np.float32)
+    ref = y.copy()
+    cblas.saxpy(n, 0.75, x, incx, ref, incy)
+    np.testing.assert_allclose(oracle.axpy(n, 0.75, x, incx, y, incy), ref, rtol=1e-6, atol=1e-6)
+    ref = y.copy()
+    cblas.scopy(n, x, incx, ref, incy)
+    np.testing.assert_array_equal(oracle.copy(n, x, incx, y, incy).astype(np.float32), ref)
+
+
+@pytest.mark.parametrize("inc", [1, 4])
+def test_oracle_scal_sdsdot_vs_cblas(cblas, inc):
+    g = rng(6)
+    n = 777
+    x = g.standard_normal(n * inc).astype(np.float32)
+    y = g.standard_normal(n * inc).astype(np.float32)
+    ref = x.copy()
+    cblas.sscal(n, -1.25, ref, inc)
+    np.testing.assert_allclose(oracle.scal(n, -1.25, x, inc), ref, rtol=1e-6, atol=0)
+    # alpha == 0 writes zeros, the value of x notwithstanding
+    ref = x.copy()
+    cblas.sscal(n, 0.0, ref, inc)
+    np.testing.assert_array_equal(oracle.scal(n, 0.0, x, inc).astype(np.float32), ref)
+    got = oracle.sdsdot(n, 0.5, x, inc, y, inc)
+    assert got == pytest.approx(cblas.sdsdot(n, 0.5, x, inc, y, inc), rel=1e-5, abs=1e-4)
+    assert oracle.sdsdot(0, 0.5, x, inc, y, inc) == 0.5
+
+
+@pytest.mark.parametrize("side,uplo", [("l", "u"), ("l", "l"), ("r", "u"), ("r", "l")])
+def test_oracle_symm_vs_cblas(cblas, side, uplo):
+    """SYMM reads only the referenced triangle of A; the other triangle holds
+    garbage that must not leak into the result."""
+    g = rng(7)
+    m, n = 37, 23
+    na = m if side == "l" else n
+    lda, ldb, ldc = na + 2, m + 1, m + 3
+    a = g.uniform(-1, 1, lda * na).astype(np.float32)
+    b = g.uniform(-1, 1, ldb * n).astype(np.float32)
+    c = g.uniform(-1, 1, ldc * n).astype(np.float32)
+    ref = c.copy()
+    cblas.ssymm(side, uplo, m, n, 1.5, a, lda, b, ldb, 0.5, ref, ldc)
+    got = oracle.symm(side, uplo, m, n, 1.5, a, lda, b, ldb, 0.5, c, ldc)
+    np.testing.assert_allclose(got, ref.reshape(n, ldc).T[:m], rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+def test_oracle_omatcopy_vs_cblas(cblas, trans):
+    g = rng(8)
+    m, n = 45, 31
+    lda = m + 3
+    ldb = (m if trans == "n" else n) + 2
+    a = g.uniform(-1, 1, lda * n).astype(np.float32)
+    out = g.uniform(-1, 1, ldb * (n if trans == "n" else m)).astype(np.float32)
+    ref = out.copy()
+    cblas.somatcopy(trans, m, n, 2.0, a, lda, ref, ldb)
+    got = oracle.omatcopy(trans, m, n, 2.0, a, lda, out, ldb)
+    np.testing.assert_array_equal(got.astype(np.float32), ref)
