@@ -320,6 +320,8 @@ __global__ void __launch_bounds__(kThreads, Blas1Occupancy<Op, T>::kCtas) blas1_
   using Acc = typename Op::Acc;
   __shared__ Acc smem[kThreads / 32];
   __shared__ bool is_last;
+  pdl_trigger();
+  pdl_wait();  // before any global memory access
   Acc acc = Op::init();
   const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t nthreads = int64_t(gridDim.x) * blockDim.x;
@@ -399,12 +401,14 @@ gbblas_status_t launch_reduce(gbblas_handle_t h, int64_t n, const T* x, int64_t 
   void* tmp = nullptr;
   GB_TRY(temp_acquire(h, sizeof(Acc) * blocks, &tmp));
   Acc* partials = static_cast<Acc*>(tmp);
-  if (vec)
-    blas1_reduce<Op, T, true, HAS_Y><<<unsigned(blocks), kThreads, 0, h->stream>>>(n, x, incx, y, incy, partials,
-                                                                                 h->tickets, result);
-  else
-    blas1_reduce<Op, T, false, HAS_Y><<<unsigned(blocks), kThreads, 0, h->stream>>>(n, x, incx, y, incy, partials,
-                                                                                  h->tickets, result);
+  // a full wave (every SM at its CTA limit) may be placed early
+  const bool early = blocks == cap;
+  const cudaError_t e =
+      vec ? launch_pdl(early, blas1_reduce<Op, T, true, HAS_Y>, dim3(unsigned(blocks)), dim3(kThreads), 0, h->stream,
+                       n, x, incx, y, incy, partials, h->tickets, result)
+          : launch_pdl(early, blas1_reduce<Op, T, false, HAS_Y>, dim3(unsigned(blocks)), dim3(kThreads), 0,
+                       h->stream, n, x, incx, y, incy, partials, h->tickets, result);
+  if (e != cudaSuccess) return cuda_fail(e, "blas1_reduce");
   return after_launch("blas1_reduce");
 }
 

@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <mutex>
 #include <string>
+#include <utility>
 
 #include "../../include/gbblas.h"
 
@@ -95,5 +96,34 @@ __host__ __device__ __forceinline__ T* vec_base(T* x, int64_t n, int64_t inc) {
 }
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// ------------------------------------------------ programmatic dependent launch --
+// A kernel launched with launch_pdl(..., early = true) may place its CTAs and
+// run up to pdl_wait() while the previous kernel on the stream drains;
+// pdl_wait() returns once every earlier grid on the stream has completed with
+// its writes visible, so stream order is kept.  It is used only for grids of
+// exactly one full wave (every SM at its resident-CTA limit), whose early
+// placement cannot come out uneven.  Both calls are no-ops for a normal
+// launch; GBBLAS_PDL=0 in the environment turns early launch off.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(bool early, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = (early && pdl_enabled()) ? 1 : 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 }  // namespace gb

@@ -4,6 +4,7 @@
 //  src/sb_handle/portblas_handle.hpp:42-100,
 //  include/sb_handle/temp_memory_pool.h:33-114).
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -16,6 +17,14 @@ static thread_local std::string g_last_error;
 static std::atomic<uint64_t> g_launches{0};
 
 void set_error(const std::string& msg) { g_last_error = msg; }
+
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("GBBLAS_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
 void clear_error() { g_last_error.clear(); }
 
 gbblas_status_t after_launch(const char* kernel) {
