@@ -185,3 +185,55 @@ def test_full_size_properties(sb, torch_cuda, n):
     assert abs(dd - nr * nr) <= 2e-6 * dd
     ref = float(torch.linalg.vector_norm(x.double()).item())
     assert abs(nr - ref) <= 1e-6 * ref
+
+
+def test_blas1_chain_in_captured_cuda_graph(torch_cuda):
+    """Full-wave BLAS-1 reductions (launched with programmatic dependent
+    launch) captured back to back into a CUDA graph and replayed twice: the
+    programmatic edges keep stream order, so every result matches the
+    oracle, and a replay after changing x sees the new x."""
+    torch = torch_cuda
+    from portblas_gb300 import blas, build
+    build.build()
+    n = 1 << 23  # a full wave of CTAs
+    g = rng(97)
+    x = g.standard_normal(n).astype(np.float32)
+    y = g.standard_normal(n).astype(np.float32)
+    s = torch.cuda.Stream()
+    h = blas.SB_Handle(s)
+    xd, yd = to_dev(x, torch), to_dev(y, torch)
+    out = torch.zeros(4, device="cuda")
+    idx = torch.zeros(2, dtype=torch.int32, device="cuda")
+
+    def chain():
+        blas._asum(h, n, xd, 1, out[0:1])
+        blas._nrm2(h, n, xd, 1, out[1:2])
+        blas._dot(h, n, xd, 1, yd, 1, out[2:3])
+        blas._iamax(h, n, xd, 1, idx[0:1])
+        blas._iamin(h, n, xd, 1, idx[1:2])
+        blas._asum(h, n, yd, 1, out[3:4])
+
+    with torch.cuda.stream(s):
+        chain()  # temp memory and kernel attributes set up outside the capture
+    s.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        chain()
+    for it in range(2):
+        if it == 1:
+            x = (x * -0.5).astype(np.float32)
+            xd.copy_(torch.from_numpy(x).cuda())
+        out.zero_()
+        idx.zero_()
+        torch.cuda.synchronize()
+        graph.replay()
+        torch.cuda.synchronize()
+        o = to_host(out)
+        i = to_host(idx)
+        assert abs(o[0] - oracle.asum(n, x, 1)) <= 1e-6 * oracle.asum(n, x, 1)
+        assert abs(o[1] - oracle.nrm2(n, x, 1)) <= 1e-6 * oracle.nrm2(n, x, 1)
+        d = oracle.dot(n, x, 1, y, 1)
+        assert abs(o[2] - d) <= 1e-6 * float(np.abs(x.astype(np.float64) * y).sum())
+        assert int(i[0]) == oracle.iamax(n, x, 1) and int(i[1]) == oracle.iamin(n, x, 1)
+        assert abs(o[3] - oracle.asum(n, y, 1)) <= 1e-6 * oracle.asum(n, y, 1)
+    h.close()
