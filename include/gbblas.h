@@ -314,7 +314,9 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
 /* A reusable grouped GEMM: the problem table is uploaded once and every run
  * replays one CUDA graph holding the persistent launch (no host work per
  * run beyond cudaGraphLaunch).  Pointers and sizes are fixed at creation;
- * the data behind them may change between runs. */
+ * the data behind them may change between runs.  After a run that
+ * gbblas_check_device_error reports as timed out, destroy and re-create the
+ * plan (its device counters may not have been reset). */
 typedef struct gbblas_grouped_plan_s* gbblas_grouped_plan_t;
 gbblas_status_t gbblas_grouped_plan_create(gbblas_handle_t h, int dtype, int64_t count, const char* transa,
                                            const char* transb, const int64_t* m, const int64_t* n,
