@@ -7,14 +7,16 @@
 // src/operations/blas3/gemm_local.hpp:438-516); each problem here keeps the
 // blas::_gemm semantics (alpha/beta rules, any transposes, column-major).
 //
-// Scheduler: the problems are ordered by decreasing k (longest tiles first,
-// so the dynamic schedule ends balanced) and their output tiles numbered in
+// Scheduler: the problems are ordered by decreasing K per tile (longest tiles
+// first, so the dynamic schedule ends balanced) and their tiles numbered in
 // that order (prefix sums of per-problem tile counts in the device problem
 // table; a tile -> problem table beside it).  Every CTA of a persistent grid
-// (a multiple of the SM count) takes the next tile number from a global
+// (one per SM, at most one per tile) takes the next tile number from a global
 // atomic counter, finds its problem, and computes the tile; no CTA ever waits
 // on another.  The last CTA to finish resets the counters, so the same launch
-// can be replayed from a CUDA graph with no host work.
+// can be replayed from a CUDA graph with no host work.  On the tcgen05 path a
+// problem whose tiles would outlast the mean work per SM gets split-K: its
+// K is cut into slices, each slice a tile of its own (plan_splits).
 //
 // Two tile methods: the tcgen05 path of grouped_tc.cuh (default: 128 x 128
 // tiles, BF16-term operands streamed by per-operand TMA maps), and a SIMT

@@ -3,9 +3,10 @@
 // Two kernels, captured together in the plan's CUDA graph:
 //
 // 1. grouped_split_kernel<T, P>: converts every operand that needs it into
-//    K-major BF16 terms [P][rows][Kp] (Kp = k rounded up to 16, zero pad),
-//    any transpose absorbed through 32 x 32 shared-memory tiles so both the
-//    strided read and the K-contiguous write are coalesced.  FP32 inputs are
+//    K-major BF16 terms [P][rows][Kp] (Kp = k rounded up to 16, zero pad):
+//    K-contiguous operands in 32-row x 128-k tiles, the others transposed
+//    through 64 x 64 shared-memory tiles, so both the strided read and the
+//    K-contiguous write are coalesced.  FP32 inputs are
 //    split into P = 3 terms with exact residuals (as in gemm_tc.cu), so the
 //    six kept term products give FP32-level accuracy at any k; BF16 inputs
 //    are one term, and a BF16 operand that is already K-contiguous with a
@@ -13,8 +14,9 @@
 //    Each element is converted once, however many output tiles read it.
 //
 // 2. grouped_tc_kernel<P>: persistent CTAs over the 128 x 128 output tiles of
-//    all problems (problems ordered by decreasing k, tiles numbered in that
-//    order, a global atomic counter hands them out).  Every operand has its
+//    all problems (problems ordered by decreasing K per tile, tiles numbered
+//    in that order, a global atomic counter hands them out; a long-K problem
+//    may have its K cut into slices, see the split-K note below).  Every operand has its
 //    own TMA tensor map (in device memory, two per problem), so the operand
 //    tiles stream in with cp.async.bulk.tensor exactly as in the dense
 //    kernel, and the pipeline never drains at a tile boundary:
@@ -24,13 +26,16 @@
 //      warp 0     producer: issues the TMA loads of each slot's k-blocks into
 //                 an S-stage mbarrier ring (the P terms of A and of B in one
 //                 3-D box each);
-//      warp 1     allocates TMEM; one lane issues tcgen05.mma (M128 N128 K16)
-//                 for every term pair, commits each stage back to the
-//                 producer and each finished chunk of CHUNK k-blocks to one of
-//                 two TMEM accumulators;
+//      warp 1     allocates TMEM; one lane issues tcgen05.mma (M128 K16;
+//                 N128 for every term pair of one or two terms, and for three
+//                 terms the six products as four MMAs, two of them N256 over
+//                 adjacent B terms), commits each stage back to the producer
+//                 and each finished chunk of CHUNK k-blocks to one of two
+//                 TMEM accumulators;
 //      warps 3-10 epilogue: tcgen05.ld of each chunk into FP32 registers
 //                 (64 columns of one output row per thread), then
-//                 alpha / beta and the stores to C, while the MMA warp is
+//                 alpha / beta and the stores to C (or, for a K slice, the
+//                 partial block and the slice fold), while the MMA warp is
 //                 already filling the other accumulator.
 // Every mbarrier wait is bounded: a wait that gives up records an error code
 // and its role stops; the others give up on their own bounded waits, the
