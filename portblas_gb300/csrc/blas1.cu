@@ -8,7 +8,8 @@
 // Nothing waits on another CTA, and the combine order depends only on
 // (n, grid), so results are deterministic run to run — unlike the float
 // atomics of portBLAS's WGAtomicReduction
-// (src/operations/blas1/WGAtomicReduction.hpp:92-138).
+// (src/operations/blas1/WGAtomicReduction.hpp:92-138).  A grid of one full
+// wave is launched with programmatic dependent launch (common.cuh).
 //
 // Operator semantics follow src/operations/blas_operators.hpp:149-316 and
 // the interface rules of src/interface/blas1_interface.hpp:117-642.

@@ -10,10 +10,12 @@
 // Pipeline per CTA (128 x BN output tile, BK = 64):
 //   warp 0      TMA producer: the P A-term tiles and P B-term tiles of one
 //               k-block per stage (128-byte swizzle, K-major);
-//   warp 1      allocates TMEM, one lane issues tcgen05.mma (M=128, N=BN,
-//               K=16) for every term pair, commits each stage back to the
-//               producer and each finished k-chunk accumulator (two TMEM
-//               buffers) to the epilogue;
+//   warp 1      allocates TMEM, one lane issues tcgen05.mma (M=128, K=16;
+//               N=BN for each term pair when P <= 2; for P = 3 the six
+//               products as four MMAs, two of them N=2*BN over the adjacent
+//               B terms 0 and 1, into two column halves), commits each stage
+//               back to the producer and each finished k-chunk accumulator
+//               (two TMEM buffers) to the epilogue;
 //   warps 2-5   epilogue: tcgen05.ld of each chunk into a per-thread FP32
 //               row, then alpha/beta and stores to column-major C (beta == 0
 //               never reads C).
