@@ -303,7 +303,11 @@ def fp64_errors(torch, inp, outs):
 
 def bench_e2e(torch, blas, sb, steps, warmup, dev):
     """Same step through the public API with host buffers: H2D of every input
-    (pinned) and D2H of every result inside the timed region."""
+    (pinned) and D2H of every result inside the timed region, as a streaming
+    caller would run it: the inputs are copied on their own stream into two
+    alternating device buffers, each op starts once its own operands have
+    landed (GEMV: A and x; BLAS-1: v and w; reductions: R), so step k+1's
+    copies overlap step k's kernels; the results go back after every step."""
     g = np.random.default_rng(7)
     host = dict(
         A=torch.from_numpy(g.uniform(-1, 1, GEMV_N * GEMV_N).astype(np.float32)).pin_memory(),
@@ -312,34 +316,61 @@ def bench_e2e(torch, blas, sb, steps, warmup, dev):
         w=torch.from_numpy(g.standard_normal(VEC_N).astype(np.float32)).pin_memory(),
         R=torch.from_numpy(g.uniform(-1, 1, RED_N * RED_N).astype(np.float32)).pin_memory(),
     )
-    dev_in = {k: torch.empty_like(v, device=dev) for k, v in host.items()}
+    dev_in = [{k: torch.empty_like(v, device=dev) for k, v in host.items()} for _ in range(2)]
     outs = dict(yn=torch.empty(GEMV_N, device=dev), yt=torch.empty(GEMV_N, device=dev),
                 s=torch.zeros(3, device=dev), i=torch.zeros(2, dtype=torch.int32, device=dev),
                 ri=torch.empty(RED_N, device=dev), ro=torch.empty(RED_N, device=dev))
     host_out = {k: torch.empty_like(v, device="cpu").pin_memory() for k, v in outs.items()}
     h2d = sum(v.numel() * v.element_size() for v in host.values())
     d2h = sum(v.numel() * v.element_size() for v in outs.values())
+    compute = torch.cuda.current_stream()
+    copy = torch.cuda.Stream()
+    ops = [step_ops(blas, sb, d, outs) for d in dev_in]
+    # inputs each op group needs, in step order: 2 GEMVs, 5 BLAS-1, 2 reductions
+    groups = [(("A", "xg"), 2), (("v", "w"), 5), (("R",), 2)]
+    consumed = [torch.cuda.Event() for _ in range(2)]
+    for e in consumed:
+        e.record(compute)
 
-    def step():
-        for k in host:
-            dev_in[k].copy_(host[k], non_blocking=True)
-        run_step(blas, sb, dev_in, outs)
-        for k in outs:
-            host_out[k].copy_(outs[k], non_blocking=True)
+    def step(k):
+        b = k & 1
+        ready = []
+        with torch.cuda.stream(copy):
+            copy.wait_event(consumed[b])  # the kernels of step k-2 are done with buffer b
+            for names, _ in groups:
+                for n in names:
+                    dev_in[b][n].copy_(host[n], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(copy)
+                ready.append(ev)
+        i = 0
+        for ev, (_, count) in zip(ready, groups):
+            compute.wait_event(ev)
+            for _, fn in ops[b][i:i + count]:
+                fn()
+            i += count
+        consumed[b].record(compute)
+        for n in outs:
+            host_out[n].copy_(outs[n], non_blocking=True)
 
-    for _ in range(warmup):
-        step()
+    for k in range(warmup):
+        step(k)
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(torch)
     torch.cuda.synchronize()
-    start.record()
-    for _ in range(steps):
-        step()
-    end.record()
+    start.record(compute)
+    copy.wait_event(start)
+    for k in range(steps):
+        step(warmup + k)
+    compute.wait_stream(copy)
+    end.record(compute)
     torch.cuda.synchronize()
     barrier(torch)
-    return dict(ms=start.elapsed_time(end) / steps, h2d=h2d, d2h=d2h)
+    # the last step's results, read back through the pipeline, against FP64
+    ref_s = float(host["v"].double().abs().sum())
+    ok = abs(float(host_out["s"][0]) - ref_s) <= 1e-5 * ref_s
+    return dict(ms=start.elapsed_time(end) / steps, h2d=h2d, d2h=d2h, asum_ok=ok)
 
 
 def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
@@ -766,7 +797,10 @@ def main():
                      "traffic": NCU_TRAFFIC.get(dom), "traffic_unit": "bytes per launch (ncu)",
                      "algorithmic_bytes": ab[dom]},
         "e2e": {"value": world * total_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-                "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]},
+                "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
+                "pipelined": "inputs copied on a second stream into two alternating buffers; "
+                             "step k+1's copies overlap step k's kernels",
+                "last_asum_matches_fp64": e2e["asum_ok"]},
         "gpu_launches": mem["launches"], "clocks": mem["clocks"], "checks": mem["checks"],
         "cpu_baseline": {"value": cpu["value"], "unit": "GB/s", "cores": cpu["cores"], "kind": "port",
                          "sample": f"{cpu['steps']} full memory-bound steps on the host (OpenBLAS CBLAS + "
