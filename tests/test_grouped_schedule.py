@@ -79,3 +79,18 @@ def test_schedule_argument_errors():
         blas.grouped_schedule([_p(4, 4, 4, ta="x")])
     with pytest.raises(blas.UnsupportedException):
         blas.grouped_schedule([_p(4, 4, 4)], dtype="float64")
+
+
+def test_splitk_switch_off_and_forced(monkeypatch):
+    """GBBLAS_GROUPED_SPLITK=0 never splits; =N cuts every problem of at
+    least N k-blocks into N slices (capped at 64); short problems keep one."""
+    probs = [_p(48, 48, 1 << 18), _p(128, 128, 4096), _p(16, 16, 64)]
+    monkeypatch.setenv("GBBLAS_GROUPED_SPLITK", "0")
+    tiles, splits = blas.grouped_schedule(probs, dtype="bfloat16")
+    assert splits == [1, 1, 1] and tiles == 3
+    monkeypatch.setenv("GBBLAS_GROUPED_SPLITK", "8")
+    tiles, splits = blas.grouped_schedule(probs, dtype="bfloat16")  # k-blocks of 64: 4096, 64, 1
+    assert splits == [8, 8, 1] and tiles == 17
+    monkeypatch.setenv("GBBLAS_GROUPED_SPLITK", "1000")
+    _, splits = blas.grouped_schedule(probs, dtype="float32")  # k-blocks of 32: 8192, 128, 2
+    assert splits == [64, 1, 1]
