@@ -17,10 +17,18 @@ the results are inside its timed region.  The SGEMM precision/throughput set
 on the tensor cores, errors against the FP64 oracle on sampled entries) and
 DGEMM 4096^3 are measured in the same run and reported under "sgemm".
 
+Also in the same run: portBLAS's plain SGEMM sample (1024^3 NN, alpha 1.5,
+beta 0.5, U[-1, 1)) for AUTO and every FP32 method, under
+"config1_sgemm_1024", with OpenBLAS sgemm beside it; the batching set under
+"batched"; the learned tile selector under "selector"; and a short "summary"
+of the GEMM figures as the line's last key.
+
 --impl reference times the reference's CPU path for the same step on the host
-cores: the CBLAS that portBLAS's tests link (numpy's bundled OpenBLAS) for
-GEMV and the BLAS-1 reductions, and the OpenMP C restatement of portBLAS's
-Reduction kernel for extension::_reduction (no CBLAS counterpart).
+cores: the CBLAS that portBLAS's tests link (numpy's bundled OpenBLAS, all
+threads) for GEMV, asum, nrm2 and dot, and FP32 OpenMP restatements of
+portBLAS's IndexMax/IndexMin and Reduction kernels (oracle/cpu_baseline.c)
+for iamax/iamin (OpenBLAS runs those on one thread) and extension::_reduction
+(no CBLAS counterpart).
 """
 from __future__ import annotations
 
@@ -458,6 +466,96 @@ def bench_sgemm(torch, blas, sb, dev, reps=3, n=8192, with_dgemm=True):
     return res
 
 
+FP32_SIMT_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal: SMs x FP32 lanes x FMA x max SM clock
+
+
+def l2_flush(torch, buf):
+    """Evicts the 129 MB L2 between timed calls by writing a larger buffer."""
+    buf.add_(1.0)
+
+
+def bench_config1(torch, blas, sb, dev, reps=30):
+    """portBLAS's plain SGEMM sample (samples/gemm.cpp:22-23): C <- 1.5 A B +
+    0.5 C, NN, M = N = K = 1024, ld 1024, entries U[-1, 1) from a fixed seed,
+    for AUTO and every FP32 method; each timed call between CUDA events after
+    an L2 flush (median); error of the whole C against FP64 (torch float64 on
+    the GPU) as max |C - C64| / (1.5 |A||B| + 0.5 |C_in|).  CPU baseline:
+    OpenBLAS sgemm on all host threads."""
+    import ctypes as C
+    from portblas_gb300 import _lib
+    L = _lib.load()
+    n = 1024
+    g = np.random.default_rng(1024)
+    a = g.uniform(-1, 1, n * n).astype(np.float32)
+    b = g.uniform(-1, 1, n * n).astype(np.float32)
+    c0 = g.uniform(-1, 1, n * n).astype(np.float32)
+    ad, bd, c0d = (torch.from_numpy(x).to(dev) for x in (a, b, c0))
+    A64, B64, C64 = (x.double().view(n, n).T for x in (ad, bd, c0d))
+    ref = 1.5 * (A64 @ B64) + 0.5 * C64
+    scale = 1.5 * (A64.abs() @ B64.abs()) + 0.5 * C64.abs()
+    del A64, B64, C64
+    flush = torch.empty(64 << 20, device=dev)  # 256 MB
+    flop = 2.0 * n ** 3
+    pk = peaks()
+    pick = C.c_int(-1)
+    L.gbblas_sgemm_selector_pick(n, n, n, b"n", b"n", n, n, n, 1, C.byref(pick))
+    out = {"workload": "sgemm NN 1024^3 alpha 1.5 beta 0.5 ld 1024, U[-1,1)", "auto_config": pick.value,
+           "l2": "flushed before every timed call"}
+    cd = torch.empty_like(c0d)
+    for name in ("auto", "fp32_simt", "split_bf16x3", "split_bf16x6"):
+        sb.set_sgemm_mode(getattr(blas.sgemm_mode_t, name))
+        cd.copy_(c0d)
+        blas._gemm(sb, "n", "n", n, n, n, 1.5, ad, n, bd, n, 0.5, cd, n)
+        err = ((cd.double().view(n, n).T - ref).abs() / scale).max().item()
+        ts = []
+        for i in range(reps + 3):
+            l2_flush(torch, flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            blas._gemm(sb, "n", "n", n, n, n, 1.5, ad, n, bd, n, 0.5, cd, n)
+            e1.record()
+            e1.synchronize()
+            if i >= 3:
+                ts.append(e0.elapsed_time(e1))
+        ms = statistics.median(ts)
+        tf = flop / (ms * 1e-3) / 1e12
+        r = {"ms": ms, "tflops": tf, "max_norm_err_vs_fp64": err}
+        if name == "fp32_simt":
+            r["roofline"] = {"bound": "fp32 pipe", "peak": FP32_SIMT_PEAK_TFLOPS, "peak_src": "nominal",
+                             "frac": tf / FP32_SIMT_PEAK_TFLOPS}
+        elif name.startswith("split"):
+            prods = 3 if name.endswith("x3") else 6
+            r["roofline"] = {"bound": "tensor", "mma_tflops": prods * tf, "peak": pk["bf16_tflops"],
+                             "peak_src": pk["src"] + " bf16 burst", "frac": prods * tf / pk["bf16_tflops"]}
+        out[name] = r
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    del flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def cpu_config1(budget_s: float = 10.0) -> dict:
+    """OpenBLAS sgemm 1024^3 NN (alpha 1.5, beta 0.5) on all host threads, median."""
+    import oracle
+    cb = oracle.CBlas()
+    cb.set_threads(os.cpu_count() or 1)
+    n = 1024
+    g = np.random.default_rng(1024)
+    a = g.uniform(-1, 1, n * n).astype(np.float32)
+    b = g.uniform(-1, 1, n * n).astype(np.float32)
+    c = g.uniform(-1, 1, n * n).astype(np.float32)
+    for _ in range(3):
+        cb.sgemm(False, False, n, n, n, 1.5, a, n, b, n, 0.5, c, n)
+    ts, t_start = [], time.perf_counter()
+    while len(ts) < 10 and time.perf_counter() - t_start < budget_s:
+        t0 = time.perf_counter()
+        cb.sgemm(False, False, n, n, n, 1.5, a, n, b, n, 0.5, c, n)
+        ts.append(time.perf_counter() - t0)
+    ms = statistics.median(ts) * 1e3
+    return {"tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "ms": ms, "cores": os.cpu_count() or 1,
+            "kind": "port", "sample": f"OpenBLAS sgemm 1024^3 NN, {len(ts)} calls, median"}
+
+
 def bench_batched(torch, blas, sb, dev, reps=10):
     """Batching workload: a grouped batch of 2048 problems with M, N, K each
     log-uniform in [16, 512] (seeded), random transposes, FP32 and BF16 inputs
@@ -657,28 +755,75 @@ def bench_selector(torch, blas, sb, dev, shapes=48):
     return out
 
 
+def summarize(c1, sg, bat, sel, pk) -> dict | None:
+    """The GEMM and batching headline figures in a few hundred bytes."""
+    if sg is None:
+        return None
+    r3 = lambda x: None if x is None else float(f"{x:.3g}")
+    out = {}
+    nn = {k: sg.get(f"{k}_NN", {}) for k in ("fp32_simt", "split_bf16x3", "split_bf16x6")}
+    tn = {k: sg.get(f"{k}_TN", {}) for k in ("fp32_simt", "split_bf16x3", "split_bf16x6")}
+    x3 = nn["split_bf16x3"]
+    out["sgemm8192_tflops"] = {k: r3(v.get("tflops")) for k, v in nn.items()}
+    out["sgemm8192_max_norm_err"] = {k: r3(max(v.get("max_norm_err", 0), tn[k].get("max_norm_err", 0)))
+                                     for k, v in nn.items()}
+    if x3.get("tflops") and nn["fp32_simt"].get("tflops"):
+        out["x3_speedup_vs_simt"] = r3(x3["tflops"] / nn["fp32_simt"]["tflops"])
+        # the dense x3 kernel issues three BF16 products per FP32 flop
+        out["x3_roofline"] = {"bound": "tensor", "achieved": r3(3 * x3["tflops"]), "peak": pk["bf16_tflops"],
+                              "unit": "TFLOP/s", "frac": r3(3 * x3["tflops"] / pk["bf16_tflops"]),
+                              "peak_src": pk["src"] + " bf16 burst"}
+    out["err_measure"] = "max |C-C64| / (|alpha||A||B| + |beta||C|)"
+    if "dgemm_4096" in sg:
+        out["dgemm4096_tflops"] = r3(sg["dgemm_4096"]["tflops"])
+    if c1:
+        out["config1"] = {k: {"tflops": r3(c1[k]["tflops"]), "err": r3(c1[k]["max_norm_err_vs_fp64"])}
+                          for k in ("auto", "fp32_simt", "split_bf16x3", "split_bf16x6")}
+        if c1.get("cpu_baseline"):
+            out["config1"]["cpu_openblas_tflops"] = r3(c1["cpu_baseline"]["tflops"])
+    if bat:
+        gr = bat["grouped"]
+        out["grouped2048"] = {dt: {"ms": r3(gr[dt]["ms"]), "tflops": r3(gr[dt]["tflops"]),
+                                   "err": r3(gr[dt]["max_norm_err_vs_fp64"])} for dt in ("float32", "bfloat16")}
+        st = bat["strided_4096x64"]
+        out["strided4096x64"] = {"ms": r3(st["ms"]), "gbs": r3(st["gbs"]), "hbm_frac": r3(st["gbs"] / pk["hbm_gbs"]),
+                                 "err": r3(st["max_norm_err_vs_fp64"])}
+    if sel:
+        out["selector_regret"] = {"live": r3(sel["live_regret_mean"]["mlp"]), "live_shapes": sel["live_shapes"]}
+        if "heldout" in sel:
+            out["selector_regret"]["heldout"] = r3(sel["heldout"]["regret_mean"]["mlp"])
+    return out
+
+
 # ----------------------------------------------------------- CPU side --
 def cpu_reference_step(cb, oracle_mod, data, outs):
-    """The memory-bound step on the host cores: OpenBLAS CBLAS + OpenMP C
-    restatement of the Reduction kernel."""
+    """The memory-bound step on the host cores: OpenBLAS CBLAS (all threads)
+    for GEMV, asum, nrm2 and dot; the FP32 OpenMP restatements of portBLAS's
+    IndexMax/IndexMin and Reduction kernels (oracle/cpu_baseline.c) for
+    iamax/iamin (OpenBLAS runs those on one thread) and the reductions (no
+    CBLAS counterpart)."""
     cb.sgemv("n", GEMV_N, GEMV_N, 1.0, data["A"], GEMV_N, data["xg"], 1, 0.0, outs["yn"], 1)
     cb.sgemv("t", GEMV_N, GEMV_N, 1.0, data["A"], GEMV_N, data["xg"], 1, 0.0, outs["yt"], 1)
     cb.sasum(VEC_N, data["v"], 1)
     cb.snrm2(VEC_N, data["v"], 1)
     cb.sdot(VEC_N, data["v"], 1, data["w"], 1)
-    cb.isamax(VEC_N, data["v"], 1)
-    np.argmin(np.abs(data["v"]))  # iamin has no CBLAS symbol: first strict minimum
-    oracle_mod.reduction("add", "inner", data["R64"], RED_N, RED_N, RED_N)
-    oracle_mod.reduction("add", "outer", data["R64"], RED_N, RED_N, RED_N)
+    oracle_mod.cpu_iamax(data["v"], is_min=False)
+    oracle_mod.cpu_iamax(data["v"], is_min=True)
+    oracle_mod.cpu_reduction_add("inner", data["R"], RED_N, RED_N, RED_N, out=outs["ri"])
+    oracle_mod.cpu_reduction_add("outer", data["R"], RED_N, RED_N, RED_N, out=outs["ro"])
+
+
+CPU_SAMPLE = ("OpenBLAS CBLAS on all host threads (sgemv N/T, sasum, snrm2, sdot) + FP32 OpenMP restatements "
+              "of portBLAS IndexMax/IndexMin (iamax, iamin) and Reduction (inner + outer, FP32 accumulate, "
+              "FP32 input)")
 
 
 def cpu_reference_data():
     g = np.random.default_rng(3)
-    R = g.uniform(-1, 1, RED_N * RED_N).astype(np.float32)
     return dict(A=g.uniform(-1, 1, GEMV_N * GEMV_N).astype(np.float32),
                 xg=g.uniform(-1, 1, GEMV_N).astype(np.float32),
                 v=g.standard_normal(VEC_N).astype(np.float32), w=g.standard_normal(VEC_N).astype(np.float32),
-                R64=R.astype(np.float64))
+                R=g.uniform(-1, 1, RED_N * RED_N).astype(np.float32))
 
 
 def bench_cpu(steps: int, warmup: int, budget_s: float = 20.0) -> dict:
@@ -687,7 +832,8 @@ def bench_cpu(steps: int, warmup: int, budget_s: float = 20.0) -> dict:
     cb = oracle.CBlas()
     cb.set_threads(cores)
     data = cpu_reference_data()
-    outs = dict(yn=np.empty(GEMV_N, np.float32), yt=np.empty(GEMV_N, np.float32))
+    outs = dict(yn=np.empty(GEMV_N, np.float32), yt=np.empty(GEMV_N, np.float32),
+                ri=np.empty(RED_N, np.float32), ro=np.empty(RED_N, np.float32))
     for _ in range(max(1, warmup)):
         cpu_reference_step(cb, oracle, data, outs)
     ts = []
@@ -736,9 +882,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                 "config": config,
                 "cpu_baseline": {"value": r["value"], "unit": "GB/s", "cores": r["cores"], "kind": "port",
-                                 "sample": "full memory-bound step on the host: numpy-bundled OpenBLAS CBLAS "
-                                           "(sgemv N/T, sasum, snrm2, sdot, isamax; iamin by first strict minimum) "
-                                           "+ OpenMP C restatement of portBLAS Reduction (FP64 accumulate)"},
+                                 "sample": f"{r['steps']} full memory-bound steps on the host, median: " + CPU_SAMPLE},
                 "e2e": {"value": r["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -773,14 +917,17 @@ def main():
     ab = algorithmic_bytes()
     dom = mem["dom"]
     achieved = ab[dom] / (mem["dom_ms"] * 1e-3) / 1e9  # its mean launch duration inside the timed region
-    sg = bat = sel = None
+    sg = bat = sel = c1 = None
     if not args.no_sgemm:
+        c1 = bench_config1(torch, blas, sb, dev)
         sg = bench_sgemm(torch, blas, sb, dev)
         bat = bench_batched(torch, blas, sb, dev)
         sel = bench_selector(torch, blas, sb, dev)
     if rank != 0:
         return
     cpu = bench_cpu(2, 1, budget_s=15.0)
+    if c1 is not None:
+        c1["cpu_baseline"] = cpu_config1()
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -803,12 +950,13 @@ def main():
                 "last_asum_matches_fp64": e2e["asum_ok"]},
         "gpu_launches": mem["launches"], "clocks": mem["clocks"], "checks": mem["checks"],
         "cpu_baseline": {"value": cpu["value"], "unit": "GB/s", "cores": cpu["cores"], "kind": "port",
-                         "sample": f"{cpu['steps']} full memory-bound steps on the host (OpenBLAS CBLAS + "
-                                   "OpenMP C Reduction restatement), median"},
+                         "sample": f"{cpu['steps']} full memory-bound steps on the host, median: " + CPU_SAMPLE},
+        "config1_sgemm_1024": c1,
         "sgemm": sg,
         "batched": bat,
         "selector": sel,
     }
+    line["summary"] = summarize(c1, sg, bat, sel, pk)  # last key: short, so that a cut tail still holds it
     print(json.dumps(line), flush=True)
 
 

@@ -186,16 +186,22 @@ gbblas_status_t gbblas_dgemv(gbblas_handle_t h, char trans, int64_t m, int64_t n
                              int64_t lda, const double* x, int64_t incx, double beta, double* y, int64_t incy);
 
 /* Allocation-free GEMV.  No counterpart in portBLAS: it is gbblas_sgemv for
- * callers that cannot allocate device memory (inside a stream capture, under
- * an allocator that owns all device memory, in hosts that forbid allocation
- * after start-up).  Same arguments and results as gbblas_sgemv, but it takes
- * the cudaStream_t directly (no handle) and its scratch is a fixed 1 MiB
- * block of file-scope device memory (plus 256 KiB of ticket counters) that
- * every GPU loading the library holds until exit; a problem needing more is
- * rejected with GBBLAS_STATUS_INVALID_ARG before anything runs.  The first
- * call on a device looks the block up (cudaGetSymbolAddress): make it before
- * any stream capture.  All calls share the block, so calls that overlap on
- * the GPU race. */
+ * callers that cannot allocate device memory — hosts whose device memory is
+ * owned by their own allocator, plug-in hosts that forbid allocation once
+ * running, latency-critical loops that cannot take cudaMalloc's implicit
+ * synchronisation.  Same arguments and results as gbblas_sgemv, but it takes
+ * the cudaStream_t directly (no handle; the stream must belong to the current
+ * device) and its scratch is a fixed 1 MiB block of file-scope device memory
+ * (plus 256 KiB of ticket counters) that every GPU loading the library holds
+ * until exit.  Argument errors are rejected before anything is enqueued; a
+ * problem needing more scratch is rejected with GBBLAS_STATUS_INVALID_ARG
+ * before any kernel runs.  Each call enqueues one cudaMemsetAsync clearing
+ * 4 bytes of tickets per output element (at most 256 KiB).  The first call on
+ * a device looks the block up (cudaGetSymbolAddress): make it before any
+ * stream capture.  All calls share the block, so calls that overlap on the
+ * GPU race.  A device-side wait that gives up (2 s) is not reported by this
+ * call (it has returned SUCCESS; y may be wrong): use gbblas_sgemv with a
+ * handle and gbblas_check_device_error where that must be seen. */
 gbblas_status_t gbblas_sgemv_noalloc(void* stream, char trans, int64_t m, int64_t n, float alpha, const float* a,
                                      int64_t lda, const float* x, int64_t incx, float beta, float* y,
                                      int64_t incy);

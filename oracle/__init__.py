@@ -37,12 +37,12 @@ DBL_MAX = float(np.finfo(np.float64).max)
 
 def build(verbose: bool = False) -> str:
     """Compile oracle.c with gcc (OpenMP, no FP contraction)."""
-    src = os.path.join(HERE, "oracle.c")
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "cpu_baseline.c")]
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+    if os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs):
         return LIB_PATH
     cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-o", LIB_PATH, src, "-lm"]
+           "-o", LIB_PATH, *srcs, "-lm"]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)
@@ -73,6 +73,10 @@ def lib():
         L.orc_iamax.restype = i64
         L.orc_reduction.argtypes = [i32, i32, P, i64, i64, i64, f64, P]
         L.orc_num_threads.restype = i32
+        L.cpu_reduction_f32.argtypes = [i32, i32, P, i64, i64, i64, P]
+        L.cpu_reduction_f32.restype = i32
+        L.cpu_iamax_f32.argtypes = [i64, P, i32]
+        L.cpu_iamax_f32.restype = i64
         _lib = L
     return _lib
 
@@ -252,6 +256,27 @@ def reduction(op: str, dim: str, inp, ld, rows, cols, dtype=np.float32):
     out = np.empty(nout)
     lib().orc_reduction(OPS[op], DIMS[dim], _p(_f64(inp)), ld, rows, cols, _tmax(dtype), _p(out))
     return out
+
+
+# ----------------------------------------- timed CPU baseline (cpu_baseline.c) --
+def cpu_reduction_add(dim: str, inp, ld, rows, cols, out=None):
+    """FP32 OpenMP restatement of portBLAS's Reduction kernel (AddOperator);
+    the timed CPU baseline, not a checker.  ``inp`` must be float32."""
+    a = np.asarray(inp)
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    nout = cols if dim == "inner" else rows
+    if out is None:
+        out = np.empty(nout, np.float32)
+    if lib().cpu_reduction_f32(0, DIMS[dim], _p(a), ld, rows, cols, _p(out)) != 0:
+        raise ValueError("cpu_reduction_f32: unsupported operator")
+    return out
+
+
+def cpu_iamax(x, is_min: bool = False) -> int:
+    """OpenMP first-index max/min |x| over a float32 vector (timed CPU baseline)."""
+    a = np.asarray(x)
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return int(lib().cpu_iamax_f32(len(a), _p(a), int(is_min)))
 
 
 def num_threads() -> int:

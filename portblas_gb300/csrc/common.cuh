@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstddef>
 #include <mutex>
@@ -96,6 +97,19 @@ __host__ __device__ __forceinline__ T* vec_base(T* x, int64_t n, int64_t inc) {
 }
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Raises `func`'s dynamic shared-memory limit to `bytes` on device `dev`.
+// The attribute belongs to each device's context, so a process driving
+// several GPUs must set it on every one: `done` is the call site's mask with
+// one bit per device (0..63; higher devices set it on every call).  Two
+// threads that race on a first call both set it, which is harmless.
+inline cudaError_t raise_smem_limit(std::atomic<uint64_t>& done, const void* func, int bytes, int dev) {
+  const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 // ------------------------------------------------ programmatic dependent launch --
 // A kernel launched with launch_pdl(..., early = true) may place its CTAs and

@@ -269,12 +269,9 @@ gbblas_status_t launch_gemm_small_batched(gbblas_handle_t h, const GemmArgs<floa
     const unsigned grid = unsigned(g.batch < cap ? g.batch : cap);
 #define GB_PIPE(TA_, TB_)                                                                                    \
   if (g.ta == TA_ && g.tb == TB_) {                                                                          \
-    static bool attr = false;                                                                                \
-    if (!attr) {                                                                                             \
-      GB_CUDA_TRY(cudaFuncSetAttribute(gemm_small_batched_pipe_kernel<TA_, TB_>,                             \
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));                  \
-      attr = true;                                                                                           \
-    }                                                                                                        \
+    static std::atomic<uint64_t> attr{0};                                                                    \
+    GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(gemm_small_batched_pipe_kernel<TA_, TB_>), \
+                                 smem, h->device));                                                          \
     gemm_small_batched_pipe_kernel<TA_, TB_><<<grid, 256, smem, h->stream>>>(g);                             \
   }
     GB_PIPE(false, false)

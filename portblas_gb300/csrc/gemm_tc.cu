@@ -364,12 +364,9 @@ static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const
                                  int64_t N, int64_t nk, int64_t batch, int split, float alpha, float beta, float* C,
                                  int64_t ldc, int64_t stride_c, float* ws, int raster_m) {
   using Cfg = TcCfg<BN, P, STAGES>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr{0};
+  GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL>),
+                               Cfg::SMEM, h->device));
   const int kb_per = int(cdiv(nk, split));
   const unsigned tn = unsigned(cdiv(N, BN)), tm = unsigned(cdiv(M, kTcBM));
   dim3 grid(raster_m ? tm : tn, raster_m ? tn : tm, unsigned(batch * split));

@@ -204,12 +204,9 @@ static gbblas_status_t launch_grouped_tc(cudaStream_t s, gbblas_grouped_plan_s* 
     grouped_split_kernel<T, P><<<unsigned(p->n_ctas), 256, 0, s>>>(p->ops, p->ctas);
     GB_TRY(after_launch("grouped_split"));
   }
-  static bool attr = false;
-  if (!attr) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(grouped_tc_kernel<P, kChunk, GroupedProblem>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<P>::SMEM));
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr{0};
+  GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(grouped_tc_kernel<P, kChunk, GroupedProblem>),
+                               GtCfg<P>::SMEM, p->device));
   grouped_tc_kernel<P, kChunk, GroupedProblem><<<p->grid, kGtThreads, GtCfg<P>::SMEM, s>>>(
       p->table, p->tile_prob, p->maps, p->total_tiles, p->counters, p->parts, p->ticks, err);
   return after_launch("grouped_tc");
@@ -766,6 +763,7 @@ gbblas_status_t gbblas_gemm_grouped(gbblas_handle_t h, int dtype, int64_t count,
   void* ws = nullptr;
   GB_TRY(temp_acquire(h, L0.total, &ws));
   gbblas_grouped_plan_s tmp;
+  tmp.device = h->device;
   const GroupedLayout L = bind_plan(h, dtype, method, H, ws, &tmp);
   if (method == 1)
     GB_TRY(encode_tc_operands(dtype, H.tab, H.operands, static_cast<uint8_t*>(ws) + L.terms, H.maps, H.ops, H.ctas));

@@ -1,25 +1,38 @@
 // noalloc.cu — a GEMV entry point that allocates no device memory.
 //
-// Some callers cannot allocate: code running inside a stream capture that
-// must not call cudaMalloc, callers whose memory is fully carved up by their
-// own allocator, or plug-in hosts that forbid allocation after start-up.
-// gbblas_sgemv_noalloc serves them.  It runs the same GEMV kernels as
-// gbblas_sgemv, but the scratch those kernels need (the split partial sums
-// and the last-CTA tickets) lives in file-scope __device__ arrays of fixed
-// size, and the handle is built on the stack around the caller's stream.
+// Some callers cannot allocate device memory: hosts whose device memory is
+// fully carved up by their own allocator (a framework's caching allocator, a
+// pool sized at start-up), plug-in hosts that forbid allocation once running,
+// and latency-critical loops that cannot take the implicit synchronisation of
+// cudaMalloc/cudaFree.  gbblas_sgemv_noalloc serves them.  It runs the same
+// GEMV kernels as gbblas_sgemv, but the scratch those kernels need (the split
+// partial sums and the last-CTA tickets) lives in file-scope __device__
+// arrays of fixed size, and the handle is built on the stack around the
+// caller's stream.
 //
 // Limits and rules (also stated in include/gbblas.h):
 //   * scratch: kNoAllocScratchBytes (1 MiB) of partial sums; a problem whose
-//     split plan needs more is rejected with GBBLAS_STATUS_INVALID_ARG
-//     before anything is launched;
+//     split plan needs more is rejected with GBBLAS_STATUS_INVALID_ARG before
+//     any kernel runs (argument errors are rejected before anything is
+//     enqueued; the ticket clear below may already be enqueued for a problem
+//     rejected for its scratch size, which changes nothing but the tickets);
 //   * every GPU that loads the library holds the arrays (1 MiB + 256 KiB)
 //     until the process exits;
 //   * the first call on each device looks up the arrays' device addresses
 //     (cudaGetSymbolAddress with that device current) — make that first
 //     call before any stream capture;
+//   * the stream must belong to the current device (INVALID_ARG otherwise);
 //   * all calls share the arrays: calls that overlap on the GPU (different
-//     streams, no ordering between them) race and give wrong results; each
-//     call clears the tickets it relies on, the partial sums need no clearing.
+//     streams, no ordering between them) race and give wrong results;
+//   * each call clears the tickets it can use (one cudaMemsetAsync of
+//     4 bytes per output element, at most 256 KiB) so that a call that failed
+//     on the device cannot leave the next one a non-zero count; the partial
+//     sums need no clearing;
+//   * a bounded device-side wait that gives up (a TMA copy that does not land
+//     within 2 s) is recorded in a per-device word that this entry point does
+//     not report: the call has already returned SUCCESS and y may be wrong.
+//     Callers that need such timeouts reported use gbblas_sgemv with a handle
+//     and gbblas_check_device_error.
 #include <mutex>
 
 #include "common.cuh"
@@ -70,8 +83,19 @@ extern "C" gbblas_status_t gbblas_sgemv_noalloc(void* stream, char trans, int64_
                                                 const float* a, int64_t lda, const float* x, int64_t incx,
                                                 float beta, float* y, int64_t incy) {
   gb::clear_error();
-  int dev = 0;
+  // the argument rules of gbblas_sgemv, checked before anything is enqueued
+  if (m < 0 || n < 0) return gb::fail(GBBLAS_STATUS_INVALID_ARG, "gemv: negative dimension");
+  if (incx == 0 || incy == 0) return gb::fail(GBBLAS_STATUS_INVALID_ARG, "gemv: zero increment");
+  if (lda < 0) return gb::fail(GBBLAS_STATUS_INVALID_ARG, "gemv: negative lda");
+  const bool tr = !(trans == 'n' || trans == 'N');
+  const int64_t xlen = tr ? m : n, ylen = tr ? n : m;
+  if (ylen == 0) return GBBLAS_STATUS_SUCCESS;
+  if (!y || (xlen > 0 && (!a || !x))) return gb::fail(GBBLAS_STATUS_INVALID_ARG, "gemv: null pointer");
+  int dev = 0, stream_dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev));
+  GB_CUDA_TRY(cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &stream_dev));
+  if (stream_dev != dev)
+    return gb::fail(GBBLAS_STATUS_INVALID_ARG, "sgemv_noalloc: the stream belongs to another device than the current one");
   DeviceArrays* d = nullptr;
   GB_TRY(device_arrays(dev, &d));
   gbblas_handle_s h;  // lives on the stack: nothing to allocate or free
@@ -85,8 +109,11 @@ extern "C" gbblas_status_t gbblas_sgemv_noalloc(void* stream, char trans, int64_
   h.n_tickets = gb::kMaxTickets;
   h.dev_error = d->error;
   h.no_alloc = true;
-  // the tickets must start at zero; the kernels reset the ones they use, this
-  // also clears any left behind by an earlier call that failed on the device
-  GB_CUDA_TRY(cudaMemsetAsync(d->tickets, 0, sizeof(unsigned int) * gb::kMaxTickets, h.stream));
+  // Tickets must start at zero.  The kernels reset the ones they use; this
+  // also clears any left behind by an earlier call that gave up on the
+  // device.  Each output tile holds at least one output element and takes at
+  // most one ticket, so the first min(ylen, kMaxTickets) are all a call uses.
+  const size_t n_clear = size_t(ylen) < gb::kMaxTickets ? size_t(ylen) : gb::kMaxTickets;
+  GB_CUDA_TRY(cudaMemsetAsync(d->tickets, 0, sizeof(unsigned int) * n_clear, h.stream));
   return gbblas_sgemv(&h, trans, m, n, alpha, a, lda, x, incx, beta, y, incy);
 }

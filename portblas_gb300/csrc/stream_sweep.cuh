@@ -474,11 +474,12 @@ inline bool try_rows_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
   // x staged only when the split's columns fit the stage
   const size_t smem = rows_tma_smem<Acc, T>(false) +
                       ((HAS_X && p.per_split <= kRowsXStage) ? sizeof(T) * size_t(p.per_split) : 0);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(rows_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(rows_tma_smem<Acc, T>(HAS_X)));
-    attr = true;
+  static std::atomic<uint64_t> attr{0};
+  const cudaError_t ae = raise_smem_limit(attr, reinterpret_cast<const void*>(rows_sweep_tma<P, T, HAS_X>),
+                                          int(rows_tma_smem<Acc, T>(HAS_X)), h->device);
+  if (ae != cudaSuccess) {
+    *st = cuda_fail(ae, "rows_sweep_tma: shared-memory limit");
+    return true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));
   rows_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(map, pol, M, N, xb, incx, p.per_split,
@@ -506,11 +507,12 @@ inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
     partials = static_cast<Acc*>(tmp);
   }
   const size_t smem = cols_tma_smem<T>(HAS_X, p.per_split);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(cols_sweep_tma<P, T, HAS_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(cols_tma_smem<T>(HAS_X, kColsXRows)));
-    attr = true;
+  static std::atomic<uint64_t> attr{0};
+  const cudaError_t ae = raise_smem_limit(attr, reinterpret_cast<const void*>(cols_sweep_tma<P, T, HAS_X>),
+                                          int(cols_tma_smem<T>(HAS_X, kColsXRows)), h->device);
+  if (ae != cudaSuccess) {
+    *st = cuda_fail(ae, "cols_sweep_tma: shared-memory limit");
+    return true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));
   cols_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(

@@ -227,3 +227,28 @@ def test_oracle_omatcopy_vs_cblas(cblas, trans):
     cblas.somatcopy(trans, m, n, 2.0, a, lda, ref, ldb)
     got = oracle.omatcopy(trans, m, n, 2.0, a, lda, out, ldb)
     np.testing.assert_array_equal(got.astype(np.float32), ref)
+
+
+@pytest.mark.parametrize("dim", ["inner", "outer"])
+@pytest.mark.parametrize("rows,cols,ld", [(1, 1, 1), (17, 5, 20), (1000, 37, 1003), (513, 1030, 513)])
+def test_cpu_baseline_reduction_matches_fp64(dim, rows, cols, ld):
+    """The timed CPU restatement of the Reduction kernel (FP32 lanes + tree)
+    agrees with an FP64 sum within FP32 accumulation error."""
+    g = np.random.default_rng(rows * 7 + cols)
+    a = g.uniform(-1, 1, ld * cols).astype(np.float32)
+    got = oracle.cpu_reduction_add(dim, a, ld, rows, cols)
+    M = a.reshape(cols, ld)[:, :rows].astype(np.float64)  # M[c, r]
+    ref = M.sum(1) if dim == "inner" else M.sum(0)
+    n_red = rows if dim == "inner" else cols
+    np.testing.assert_allclose(got, ref, rtol=0, atol=4 * n_red * 2.0 ** -24 * np.abs(M).max() + 1e-7)
+
+
+@pytest.mark.parametrize("n", [1, 2, 1000, 100003])
+def test_cpu_baseline_iamax_iamin_first_index(n):
+    g = np.random.default_rng(n)
+    x = g.standard_normal(n).astype(np.float32)
+    if n > 10:
+        x[[3, n // 2, n - 1]] = 7.5   # ties: the first index wins
+        x[[5, n // 3]] = 0.0
+    assert oracle.cpu_iamax(x) == int(np.argmax(np.abs(x)))
+    assert oracle.cpu_iamax(x, is_min=True) == int(np.argmin(np.abs(x)))

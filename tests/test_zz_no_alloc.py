@@ -1,10 +1,11 @@
 """The allocation-free GEMV entry point (gbblas_sgemv_noalloc).
 
-It exists for callers that cannot allocate device memory — inside a stream
-capture, under an allocator that owns all device memory, or in hosts that
-forbid allocation once running.  Called here through the C ABI and compared
-with gbblas_sgemv (the regular, allocating entry point) on two calls in a row,
-at the GEMV tests' tolerance.  This file is collected last so that a run that
+It exists for callers that cannot allocate device memory: hosts whose GPU
+memory is owned by an allocator of their own, plug-in hosts that forbid
+allocation once running, and loops that cannot take cudaMalloc's implicit
+synchronisation.  Called here through the C ABI and compared with
+gbblas_sgemv (the regular, allocating entry point) on two calls in a row, at
+the GEMV tests' tolerance.  This file is collected last so that a run that
 stops at the first failure has already run every other test.
 """
 import ctypes as C
@@ -66,4 +67,15 @@ def test_noalloc_rejects_scratch_beyond_maximum(L, torch_cuda):
     st = L.gbblas_sgemv_noalloc(_stream(torch), b"t", m, n, 1.0, p, m, p, 1, 0.0, p, 1)
     assert st == 1
     assert b"allocation-free maximum" in L.gbblas_last_error()
+    torch.cuda.synchronize()
+
+
+def test_noalloc_rejects_bad_arguments_before_enqueueing(L, torch_cuda):
+    """Argument errors come back as INVALID_ARG, as from gbblas_sgemv."""
+    torch = torch_cuda
+    buf = torch.zeros(64, device="cuda")
+    p = buf.data_ptr()
+    assert L.gbblas_sgemv_noalloc(_stream(torch), b"n", -1, 4, 1.0, p, 4, p, 1, 0.0, p, 1) == 1
+    assert L.gbblas_sgemv_noalloc(_stream(torch), b"n", 4, 4, 1.0, p, 4, p, 0, 0.0, p, 1) == 1
+    assert L.gbblas_sgemv_noalloc(_stream(torch), b"n", 4, 4, 1.0, None, 4, p, 1, 0.0, p, 1) == 1
     torch.cuda.synchronize()
