@@ -7,16 +7,19 @@
  *   include/interface/blas1_interface.h   (_asum, _nrm2, _dot, _iamax, _iamin,
  *                                          _scal, _axpy, _copy, _sdsdot)
  *   include/interface/blas2_interface.h   (_gemv)
- *   include/interface/blas3_interface.h   (_gemm, _gemm_batched, _gemm_strided_batched, _symm)
+ *   include/interface/blas3_interface.h   (_gemm, _gemm_batched, _gemm_strided_batched, _symm;
+ *                                          extension::_gemm_grouped has no portBLAS counterpart)
  *   include/interface/extension_interface.h (extension::_reduction, _omatcopy, _transpose)
  * and the errors are the same exception types (std::invalid_argument,
  * blas::unsupported_exception).  Differences a caller can observe:
  *   - SB_Handle wraps a cudaStream_t instead of a sycl::queue, and buffers are
  *     device pointers (portBLAS's USM mode); there is no BufferIterator.
- *   - event_t is a vector of cudaEvent_t.  Each call makes its stream wait on
- *     the dependency events and returns one event recorded after its work;
- *     returned events come from a ring of kEventRing per handle and stay valid
- *     for the next kEventRing - 1 calls on that handle.
+ *   - event_t is a vector of blas::event, each owning one recorded CUDA event
+ *     (converts to cudaEvent_t).  Each call makes its stream wait on the
+ *     dependency events and returns one event recorded after its work.  An
+ *     event stays valid, and refers to its own point in the stream, for as
+ *     long as a copy of it is held; its cudaEvent_t is reused for a later
+ *     call only after the last copy is gone (also after the handle is gone).
  *   - the async BLAS-1 reductions overwrite the result (portBLAS adds into it).
  */
 #ifndef PORTBLAS_GB_H
@@ -24,9 +27,13 @@
 
 #include <cuda_runtime_api.h>
 
+#include <cstdint>
+#include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "gbblas.h"
@@ -66,23 +73,68 @@ template <typename C>
 using elem_t = std::remove_cv_t<std::remove_pointer_t<C>>;
 }  // namespace detail
 
+namespace detail {
+/* Recycled CUDA events of one handle.  Shared by the handle and by every
+ * event it handed out, so it lives until the last of them is gone. */
+class EventPool {
+ public:
+  ~EventPool() {
+    for (cudaEvent_t e : free_) cudaEventDestroy(e);
+  }
+  cudaEvent_t acquire() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!free_.empty()) {
+        cudaEvent_t e = free_.back();
+        free_.pop_back();
+        return e;
+      }
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      throw std::runtime_error("SB_Handle: cudaEventCreate failed");
+    return e;
+  }
+  void release(cudaEvent_t e) {
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.push_back(e);
+  }
+
+ private:
+  std::mutex mu_;
+  std::vector<cudaEvent_t> free_;
+};
+}  // namespace detail
+
+/* One point in a handle's stream, as a sycl::event is one submitted command
+ * group.  Copies share the CUDA event; it goes back to its handle's pool when
+ * the last copy is destroyed. */
+class event {
+ public:
+  event() = default;
+  explicit event(std::shared_ptr<CUevent_st> e) : e_(std::move(e)) {}
+  cudaEvent_t get() const { return e_.get(); }
+  operator cudaEvent_t() const { return e_.get(); }
+  void wait() const {
+    if (e_ && cudaEventSynchronize(e_.get()) != cudaSuccess) throw std::runtime_error("blas::event::wait failed");
+  }
+  /* sycl::event::get_info<command_execution_status> counterpart: true once
+   * the work before the event has finished. */
+  bool is_complete() const { return !e_ || cudaEventQuery(e_.get()) == cudaSuccess; }
+
+ private:
+  std::shared_ptr<CUevent_st> e_;
+};
+
 /* blas::SB_Handle (include/sb_handle/portblas_handle.h:46-200) over a CUDA stream. */
 class SB_Handle {
  public:
-  using event_t = std::vector<cudaEvent_t>;
-  static constexpr int kEventRing = 64;
+  using event_t = std::vector<event>;
 
-  explicit SB_Handle(cudaStream_t stream = nullptr) : stream_(stream) {
+  explicit SB_Handle(cudaStream_t stream = nullptr) : stream_(stream), pool_(std::make_shared<detail::EventPool>()) {
     detail::check(gbblas_handle_create(static_cast<void*>(stream), &h_));
-    for (auto& e : ring_)
-      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-        throw std::runtime_error("SB_Handle: cudaEventCreate failed");
   }
-  ~SB_Handle() {
-    for (auto& e : ring_)
-      if (e) cudaEventDestroy(e);
-    gbblas_handle_destroy(h_);
-  }
+  ~SB_Handle() { gbblas_handle_destroy(h_); }
   SB_Handle(const SB_Handle&) = delete;
   SB_Handle& operator=(const SB_Handle&) = delete;
 
@@ -90,29 +142,31 @@ class SB_Handle {
   gbblas_handle_t native() const { return h_; }
   void wait() { detail::check(gbblas_wait(h_)); }
   void wait(const event_t& evs) {
-    for (auto e : evs)
-      if (cudaEventSynchronize(e) != cudaSuccess) throw std::runtime_error("SB_Handle::wait: event failed");
+    for (const event& e : evs) e.wait();
   }
   void set_sgemm_mode(gbblas_sgemm_mode_t m) { detail::check(gbblas_set_sgemm_mode(h_, m)); }
 
   // stream waits for the dependencies; returns an event after `status`'s work
   void depend(const event_t& deps) {
-    for (auto e : deps)
-      if (e && cudaStreamWaitEvent(stream_, e, 0) != cudaSuccess)
+    for (const event& e : deps)
+      if (e.get() && cudaStreamWaitEvent(stream_, e.get(), 0) != cudaSuccess)
         throw std::runtime_error("SB_Handle: cudaStreamWaitEvent failed");
   }
   event_t done(gbblas_status_t status) {
     detail::check(status);
-    cudaEvent_t e = ring_[next_++ % kEventRing];
-    if (cudaEventRecord(e, stream_) != cudaSuccess) throw std::runtime_error("SB_Handle: cudaEventRecord failed");
-    return event_t{e};
+    cudaEvent_t raw = pool_->acquire();
+    if (cudaEventRecord(raw, stream_) != cudaSuccess) {
+      pool_->release(raw);
+      throw std::runtime_error("SB_Handle: cudaEventRecord failed");
+    }
+    std::shared_ptr<detail::EventPool> pool = pool_;
+    return event_t{event(std::shared_ptr<CUevent_st>(raw, [pool](CUevent_st* p) { pool->release(p); }))};
   }
 
  private:
   cudaStream_t stream_;
   gbblas_handle_t h_ = nullptr;
-  cudaEvent_t ring_[kEventRing] = {};
-  unsigned next_ = 0;
+  std::shared_ptr<detail::EventPool> pool_;
 };
 
 /* ------------------------------------------------------------------ BLAS-3 */
@@ -423,6 +477,87 @@ typename sb_handle_t::event_t _transpose(sb_handle_t& sb, index_t m, index_t n, 
   else
     throw unsupported_exception("_transpose: element type not supported");
 }
+/* Uneven batched GEMM.  No portBLAS counterpart: portBLAS batches only
+ * problems of one size (_gemm_batched, include/interface/blas3_interface.h:
+ * 97-109).  `group_count` independent problems of any sizes,
+ * C_i <- alpha_i op_i(A_i) op_i(B_i) + beta_i C_i, run as one persistent
+ * tensor-core launch with FP32 accumulation.  A and B are float, or any
+ * 2-byte type holding bfloat16 bits (__nv_bfloat16, uint16_t); C is float.
+ * transa/transb hold one 'n'/'t'/'c' per problem; every other argument is an
+ * array of group_count host values. */
+namespace grouped {
+template <typename in_t>
+constexpr int grouped_dtype() {
+  static_assert(std::is_same_v<in_t, float> || sizeof(in_t) == 2,
+                "_gemm_grouped: A and B must be float or 2-byte bfloat16");
+  return std::is_same_v<in_t, float> ? GBBLAS_DTYPE_F32 : GBBLAS_DTYPE_BF16;
+}
+/* host copies of the per-problem arrays in the C ABI's types */
+struct GroupedArgs {
+  std::vector<int64_t> m, n, k, lda, ldb, ldc;
+  std::vector<float> alpha, beta;
+  std::vector<const void*> a, b;
+  template <typename index_t, typename element_t, typename in_t>
+  GroupedArgs(index_t count, const index_t* m_, const index_t* n_, const index_t* k_, const element_t* alpha_,
+              const in_t* const* a_, const index_t* lda_, const in_t* const* b_, const index_t* ldb_,
+              const element_t* beta_, const index_t* ldc_) {
+    if (count < 0) throw std::invalid_argument("_gemm_grouped: negative group count");
+    const size_t c = size_t(count);
+    if (c && (!m_ || !n_ || !k_ || !alpha_ || !a_ || !lda_ || !b_ || !ldb_ || !beta_ || !ldc_))
+      throw std::invalid_argument("_gemm_grouped: null argument array");
+    m.assign(m_, m_ + c), n.assign(n_, n_ + c), k.assign(k_, k_ + c);
+    lda.assign(lda_, lda_ + c), ldb.assign(ldb_, ldb_ + c), ldc.assign(ldc_, ldc_ + c);
+    alpha.assign(alpha_, alpha_ + c), beta.assign(beta_, beta_ + c);
+    a.assign(a_, a_ + c), b.assign(b_, b_ + c);
+  }
+};
+}  // namespace grouped
+
+template <typename sb_handle_t, typename in_t, typename index_t, typename element_t>
+typename sb_handle_t::event_t _gemm_grouped(sb_handle_t& sb, index_t group_count, const char* transa,
+                                            const char* transb, const index_t* m, const index_t* n, const index_t* k,
+                                            const element_t* alpha, const in_t* const* a, const index_t* lda,
+                                            const in_t* const* b, const index_t* ldb, const element_t* beta,
+                                            float* const* c, const index_t* ldc,
+                                            const typename sb_handle_t::event_t& deps = {}) {
+  grouped::GroupedArgs g(group_count, m, n, k, alpha, a, lda, b, ldb, beta, ldc);
+  sb.depend(deps);
+  return sb.done(gbblas_gemm_grouped(sb.native(), grouped::grouped_dtype<in_t>(), int64_t(group_count), transa,
+                                     transb, g.m.data(), g.n.data(), g.k.data(), g.alpha.data(), g.a.data(),
+                                     g.lda.data(), g.b.data(), g.ldb.data(), g.beta.data(), c, g.ldc.data()));
+}
+
+/* A reusable _gemm_grouped: the problem table goes to the device once, and
+ * each run() replays one CUDA graph.  Pointers and sizes are fixed at
+ * construction; the data behind them may change between runs. */
+template <typename in_t>
+class gemm_grouped_plan {
+ public:
+  template <typename sb_handle_t, typename index_t, typename element_t>
+  gemm_grouped_plan(sb_handle_t& sb, index_t group_count, const char* transa, const char* transb, const index_t* m,
+                    const index_t* n, const index_t* k, const element_t* alpha, const in_t* const* a,
+                    const index_t* lda, const in_t* const* b, const index_t* ldb, const element_t* beta,
+                    float* const* c, const index_t* ldc) {
+    grouped::GroupedArgs g(group_count, m, n, k, alpha, a, lda, b, ldb, beta, ldc);
+    ::blas::detail::check(gbblas_grouped_plan_create(sb.native(), grouped::grouped_dtype<in_t>(), int64_t(group_count), transa,
+                                             transb, g.m.data(), g.n.data(), g.k.data(), g.alpha.data(),
+                                             g.a.data(), g.lda.data(), g.b.data(), g.ldb.data(), g.beta.data(), c,
+                                             g.ldc.data(), &plan_));
+  }
+  ~gemm_grouped_plan() { gbblas_grouped_plan_destroy(plan_); }
+  gemm_grouped_plan(const gemm_grouped_plan&) = delete;
+  gemm_grouped_plan& operator=(const gemm_grouped_plan&) = delete;
+
+  template <typename sb_handle_t>
+  typename sb_handle_t::event_t run(sb_handle_t& sb, const typename sb_handle_t::event_t& deps = {}) {
+    sb.depend(deps);
+    return sb.done(gbblas_grouped_plan_run(sb.native(), plan_));
+  }
+
+ private:
+  gbblas_grouped_plan_t plan_ = nullptr;
+};
+
 /* include/interface/extension_interface.h:453-462 */
 template <typename operator_t, typename element_t, typename sb_handle_t, typename input_t, typename output_t,
           typename index_t>

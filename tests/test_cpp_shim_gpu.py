@@ -21,12 +21,12 @@ def _compile(src, out):
 
 def test_shim_compiles_without_gpu(tmp_path):
     build.build()
-    for s in ("gemm.cpp", "gemv.cpp", "blas_ext.cpp"):
+    for s in ("gemm.cpp", "gemv.cpp", "blas_ext.cpp", "gemm_grouped.cpp"):
         _compile(os.path.join(ROOT, "samples", s), str(tmp_path / s.replace(".cpp", "")))
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("sample", ["gemm", "gemv", "blas_ext"])
+@pytest.mark.parametrize("sample", ["gemm", "gemv", "blas_ext", "gemm_grouped"])
 def test_shim_samples_run(torch_cuda, tmp_path, sample):
     build.build()
     exe = str(tmp_path / sample)
