@@ -229,6 +229,14 @@ __global__ void __launch_bounds__(256, kPipeCtasPerSm) gemm_small_batched_pipe_k
     // C(i, j) for i = 4ty.., j = 4tx..: each column's 4 rows as one 128-bit access
     float* C = g.c + p * g.stride_c;
     if (4 * ty < M) {
+      // the four columns of C are loaded before any store so the loads overlap
+      float4 o[4];
+      if (g.beta != 0.f) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          o[j] = (4 * tx + j < N) ? *reinterpret_cast<const float4*>(C + 4 * ty + int64_t(4 * tx + j) * g.ldc)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int gj = 4 * tx + j;
@@ -236,11 +244,10 @@ __global__ void __launch_bounds__(256, kPipeCtasPerSm) gemm_small_batched_pipe_k
           float4* cp = reinterpret_cast<float4*>(C + 4 * ty + int64_t(gj) * g.ldc);
           float4 v = make_float4(g.alpha * acc[0][j], g.alpha * acc[1][j], g.alpha * acc[2][j], g.alpha * acc[3][j]);
           if (g.beta != 0.f) {
-            const float4 o = *cp;
-            v.x = fmaf(g.beta, o.x, v.x);
-            v.y = fmaf(g.beta, o.y, v.y);
-            v.z = fmaf(g.beta, o.z, v.z);
-            v.w = fmaf(g.beta, o.w, v.w);
+            v.x = fmaf(g.beta, o[j].x, v.x);
+            v.y = fmaf(g.beta, o[j].y, v.y);
+            v.z = fmaf(g.beta, o[j].z, v.z);
+            v.w = fmaf(g.beta, o[j].w, v.w);
           }
           *cp = v;
         }

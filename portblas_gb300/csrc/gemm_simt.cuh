@@ -217,19 +217,29 @@ __global__ void __launch_bounds__(kSimtThreads) gemm_simt_kernel(GemmArgs<T> g, 
     }
     return;
   }
+  // C is read one column of the micro-tile at a time, all TM loads before
+  // the stores, so the loads overlap (a store may alias a later load when
+  // ldc == 0, so the compiler cannot reorder them itself)
   T* C = g.c + bz * g.stride_c;
 #pragma unroll
   for (int j = 0; j < TN; ++j) {
     const int64_t gn = n0 + (j / 4) * (BN / QN) + tx * 4 + (j % 4);
     if (gn >= g.n) continue;
+    T cv[TM];
+    if (g.beta != T(0)) {
+#pragma unroll
+      for (int i = 0; i < TM; ++i) {
+        const int64_t gm = m0 + (i / 4) * (BM / QM) + ty * 4 + (i % 4);
+        cv[i] = gm < g.m ? C[gm + gn * g.ldc] : T(0);
+      }
+    }
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       const int64_t gm = m0 + (i / 4) * (BM / QM) + ty * 4 + (i % 4);
       if (gm >= g.m) continue;
-      T* cp = C + gm + gn * g.ldc;
       T r = g.alpha * acc[i][j];
-      if (g.beta != T(0)) r = fma(g.beta, *cp, r);
-      *cp = r;
+      if (g.beta != T(0)) r = fma(g.beta, cv[i], r);
+      C[gm + gn * g.ldc] = r;
     }
   }
 }

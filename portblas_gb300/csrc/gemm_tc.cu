@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  pdl_wait();  // the operand terms (and C) are written by earlier kernels on the stream
 
   if (warp == 0) {
     if (lane == 0) {
@@ -250,15 +251,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if (gn < N) W0[int64_t(gm) + int64_t(gn) * M] = sum[i];
         }
       } else {
-        float* Cb = C + int64_t(bz) * stride_c;
+        // C is read 32 columns at a time, all loads before any store, so the
+        // loads overlap (a store may alias a later load when ldc == 0, so the
+        // compiler cannot reorder them itself); beta == 0 never reads C
+        float* rowp = C + int64_t(bz) * stride_c + int64_t(gm);
 #pragma unroll
-        for (int i = 0; i < BN; ++i) {
-          const int gn = n0 + i;
-          if (gn < N) {
-            float* cp = Cb + int64_t(gm) + int64_t(gn) * ldc;
-            float v = alpha * sum[i];
-            if (beta != 0.f) v = fmaf(beta, *cp, v);
-            *cp = v;
+        for (int g0 = 0; g0 < BN; g0 += 32) {
+          float cv[32];
+          if (beta != 0.f) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) cv[i] = (n0 + g0 + i < N) ? rowp[int64_t(n0 + g0 + i) * ldc] : 0.f;
+          }
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const int gn = n0 + g0 + i;
+            if (gn < N) {
+              float v = alpha * sum[g0 + i];
+              if (beta != 0.f) v = fmaf(beta, cv[i], v);
+              rowp[int64_t(gn) * ldc] = v;
+            }
           }
         }
       }
@@ -280,6 +291,7 @@ template <int P>
 __global__ void __launch_bounds__(256) split_bf16_kernel(const float* __restrict__ X, int64_t sr, int64_t sk,
                                                          int64_t R, int64_t K, int64_t Kp, int64_t xstride,
                                                          __nv_bfloat16* __restrict__ out) {
+  pdl_trigger();  // the GEMM that reads the terms may place its CTAs and set up meanwhile
   __shared__ float t[32][33];  // t[k][r]
   X += int64_t(blockIdx.z) * xstride;
   out += int64_t(blockIdx.z) * P * R * Kp;
@@ -371,8 +383,11 @@ static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const
   const unsigned tn = unsigned(cdiv(N, BN)), tm = unsigned(cdiv(M, kTcBM));
   dim3 grid(raster_m ? tm : tn, raster_m ? tn : tm, unsigned(batch * split));
   if (grid.y > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
-  gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL><<<grid, kTcThreads, Cfg::SMEM, h->stream>>>(
-      ta, tb, int(M), int(N), int(nk), split, kb_per, alpha, beta, C, ldc, stride_c, ws, raster_m, h->dev_error);
+  // launched early (PDL): its CTAs set up while the split pass drains
+  const cudaError_t le = launch_pdl(true, gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL>, grid, dim3(kTcThreads),
+                                    size_t(Cfg::SMEM), h->stream, ta, tb, int(M), int(N), int(nk), split, kb_per,
+                                    alpha, beta, C, ldc, stride_c, ws, raster_m, h->dev_error);
+  if (le != cudaSuccess) return cuda_fail(le, "gemm_split_bf16");
   return after_launch("gemm_split_bf16");
 }
 
@@ -424,8 +439,23 @@ gbblas_status_t launch_gemm_split_bf16_cfg(gbblas_handle_t h, const GemmArgs<flo
   return fail(GBBLAS_STATUS_INVALID_ARG, "split-BF16 GEMM: N tile must be 64 or 128");
 }
 
+// The fixed split-BF16 modes: 128 x 128 tiles when they fill the SMs; else
+// 128 x 64 tiles; and when even those leave half the SMs idle, split-K
+// slices of at least 4 k-blocks.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
-  return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 0);
+  const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
+  const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
+  if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 0);
+  const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
+  int64_t split = 1;
+  if (2 * t64 <= sm) {
+    split = sm / t64;
+    const int64_t deep = cdiv(g.k, kTcBK) / 4;
+    if (split > deep) split = deep;
+    if (split > 16) split = 16;
+    if (split < 1) split = 1;
+  }
+  return launch_gemm_split_bf16_cfg(h, g, pieces, 64, int(split), 0);
 }
 
 }  // namespace gb

@@ -112,18 +112,23 @@ __device__ void grouped_tile(const GroupedProblem& p, int tm, int tn, float (&As
     }
     __syncthreads();
   }
+  // each column's 4 C values are loaded before its stores so the loads overlap
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int gn = n0 + tx * 4 + j;
     if (gn >= p.n) continue;
+    float cv[4];
+    if (p.beta != 0.f) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cv[i] = (m0 + ty * 4 + i < p.m) ? p.c[m0 + ty * 4 + i + int64_t(gn) * p.ldc] : 0.f;
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int gm = m0 + ty * 4 + i;
       if (gm >= p.m) continue;
-      float* cp = p.c + gm + int64_t(gn) * p.ldc;
       float v = p.alpha * acc[i][j];
-      if (p.beta != 0.f) v = fmaf(p.beta, *cp, v);
-      *cp = v;
+      if (p.beta != 0.f) v = fmaf(p.beta, cv[i], v);
+      p.c[gm + int64_t(gn) * p.ldc] = v;
     }
   }
 }

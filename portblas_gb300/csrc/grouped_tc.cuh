@@ -658,13 +658,23 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         const int64_t ldc = w.ldc;
         const float alpha = w.alpha, beta = w.beta;
         const int nleft = w.n - w.n0 - h * 64;
-        float* cp = c + gm + (int64_t(w.n0) + h * 64) * ldc;
+        float* const cp = c + gm + (int64_t(w.n0) + h * 64) * ldc;
+        // C is read 32 columns at a time, all loads before any store, so the
+        // loads overlap (a store may alias a later load when ldc == 0)
 #pragma unroll
-        for (int j = 0; j < 64; ++j, cp += ldc) {
-          if (j < nleft) {
-            float v = alpha * sum[j];
-            if (beta != 0.f) v = fmaf(beta, *cp, v);
-            *cp = v;
+        for (int j0 = 0; j0 < 64; j0 += 32) {
+          float cv[32];
+          if (beta != 0.f) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) cv[j] = (j0 + j < nleft) ? cp[int64_t(j0 + j) * ldc] : 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            if (j0 + j < nleft) {
+              float v = alpha * sum[j0 + j];
+              if (beta != 0.f) v = fmaf(beta, cv[j], v);
+              cp[int64_t(j0 + j) * ldc] = v;
+            }
           }
         }
       }

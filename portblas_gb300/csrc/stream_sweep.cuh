@@ -30,8 +30,8 @@ enum : int { kErrSweepFull = 201, kErrSweepEmpty = 202, kErrSweepDrain = 203, kE
 
 // x elements staged in shared memory by the rows sweep (one column split)
 constexpr int64_t kRowsXStage = 8192;
-// rows per chunk of the cols sweep when x is staged (16 KB of FP32 x)
-constexpr int64_t kColsXRows = 4096;
+// bytes of x a cols-sweep CTA stages in shared memory (one row chunk's x)
+constexpr int64_t kColsXBytes = 16384;
 
 // barrier among the 8 consumer warps only (the producer keeps streaming)
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -122,6 +122,7 @@ __global__ void __launch_bounds__(kStThreads)
     rows_sweep_tma(const __grid_constant__ CUtensorMap tmA, P pol, int64_t M, int64_t N, const T* __restrict__ xb,
                    int64_t incx, int64_t cols_per_split, typename P::Acc* __restrict__ partials,
                    unsigned int* __restrict__ tickets, int* __restrict__ err) {
+  pdl_trigger();
   using Acc = typename P::Acc;
   constexpr int RPT = Pack16<T>::n;
   constexpr int BM = 32 * RPT;
@@ -151,6 +152,7 @@ __global__ void __launch_bounds__(kStThreads)
     tc::fence_mbar_init();
   }
   __syncthreads();
+  pdl_wait();  // A, x, the partials and the tickets belong to earlier kernels on the stream
 
   // x of this column split goes to shared memory while the first tiles land
   const bool xstaged = HAS_X && cols_per_split <= kRowsXStage;
@@ -225,17 +227,20 @@ __global__ void __launch_bounds__(kStThreads)
 }
 
 // ------------------------------------------------------------ cols sweep --
-// CTA: `ctiles` consecutive 16-column tiles x one chunk of rows; each tile is
-// BR rows (1 KB) x 16 columns and the producer streams the chunk's row tiles
-// of each column tile in turn.  Consumer warp w folds columns 2w and 2w+1 of
+// CTA: a range of consecutive 16-column tiles x one chunk of rows; each tile
+// is BR rows (1 KB) x 16 columns and the producer streams the chunk's row
+// tiles of each column tile in turn.  The column tiles are dealt out in
+// gridDim.x ranges that differ by at most one tile (range b starts at tile
+// b * coltiles / gridDim.x), so a grid of exactly one wave is balanced.  Consumer warp w folds columns 2w and 2w+1 of
 // a tile; lane l reads rows l*RPT + {0, 32*RPT} (two 128-bit shared loads
 // per column) and the matching x from the chunk's copy of x in shared memory
 // (staged once per CTA while the first tiles land).
 template <class P, typename T, bool HAS_X>
 __global__ void __launch_bounds__(kStThreads)
     cols_sweep_tma(const __grid_constant__ CUtensorMap tmA, P pol, int64_t M, int64_t N, const T* __restrict__ xb,
-                   int64_t incx, int64_t rows_per_split, int ctiles, typename P::Acc* __restrict__ partials,
+                   int64_t incx, int64_t rows_per_split, typename P::Acc* __restrict__ partials,
                    unsigned int* __restrict__ tickets, int* __restrict__ err) {
+  pdl_trigger();
   using Acc = typename P::Acc;
   constexpr int RPT = Pack16<T>::n;
   constexpr int BR = 64 * RPT;                                  // 1 KB of rows
@@ -250,8 +255,9 @@ __global__ void __launch_bounds__(kStThreads)
   __shared__ unsigned long long last_mask;  // bit c: this CTA folds column tile ct0 + c
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t ct0 = int64_t(blockIdx.x) * ctiles;          // first column tile of this CTA
-  const int nct = int(min(int64_t(ctiles), cdiv(N, BC) - ct0));
+  const int64_t coltiles = cdiv(N, BC);
+  const int64_t ct0 = int64_t(blockIdx.x) * coltiles / gridDim.x;  // first column tile of this CTA
+  const int nct = int((int64_t(blockIdx.x) + 1) * coltiles / gridDim.x - ct0);
   const int64_t r0 = int64_t(blockIdx.y) * rows_per_split;
   const int64_t rlen = min(M - r0, rows_per_split);
   const int nrt = int(cdiv(rlen, BR));  // row tiles per column tile
@@ -264,6 +270,7 @@ __global__ void __launch_bounds__(kStThreads)
     tc::fence_mbar_init();
   }
   __syncthreads();
+  pdl_wait();  // A, x, the partials and the tickets belong to earlier kernels on the stream
 
   // the chunk's x (zero past the matrix) is staged while the first tiles land
   const XStage<T> xst(HAS_X ? xb + r0 * incx : xb, rlen, int64_t(nrt) * BR, incx);
@@ -406,36 +413,42 @@ inline size_t cols_tma_smem(bool has_x, int64_t rows_per_split) {
 }
 
 struct TmaPlan {
-  int64_t tiles, split, per_split;
-  int ctiles;  // cols sweep: column tiles per CTA
+  int64_t tiles, split, per_split;  // grid.x, grid.y, columns (rows sweep) or rows (cols sweep) per split
+  bool full_wave;                   // the grid fills (nearly) every resident slot: launched early (PDL)
 };
 
 // rows sweep: 3 resident CTAs per SM
 inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes) {
   const int64_t BM = 512 / elem_bytes, BC = kStTileBytes / 512;
+  const int64_t slots = int64_t(sm_count) * 3;
   TmaPlan p;
   p.tiles = cdiv(M, BM);
   // fill the 3 resident CTAs per SM in one wave
-  int64_t split = (int64_t(sm_count) * 3) / p.tiles;
+  int64_t split = slots / p.tiles;
   const int64_t max_split = cdiv(N, 4 * BC);  // at least 4 tiles per CTA
   if (split > max_split) split = max_split;
   if (split < 1 || p.tiles > int64_t(kMaxTickets)) split = 1;
   p.per_split = cdiv(cdiv(N, split), BC) * BC;
   p.split = cdiv(N, p.per_split);
+  const int64_t grid = p.tiles * p.split;
+  p.full_wave = grid <= slots && 32 * grid >= 31 * slots;
   return p;
 }
 
-// cols sweep: rows split into chunks (a multiple of the 1 KB tile; with x
-// at most kColsXRows rows so the chunk of x fits in shared memory), then each CTA
-// takes `ctiles` column tiles so the grid is about one wave of resident CTAs.
+// cols sweep: rows split into chunks (a multiple of the 1 KB tile; with x at
+// most kColsXBytes of x per chunk so it fits in shared memory), then the
+// column tiles are dealt out in `tiles` ranges per chunk, about `ctiles`
+// each, so the grid is about one wave of resident CTAs (3 per SM with the
+// 64 KB ring alone, 2 with x).  Finer row chunks (more CTAs, a full wave)
+// were measured slower: their partial sums and the fold at the end cost
+// more than the extra CTAs gain (GEMV 't' 8192^2 47.5 against 44.3 us).
 inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes, bool has_x) {
   const int64_t BR = 1024 / elem_bytes, BC = kStTileBytes / 1024;
-  // resident CTAs per SM: 3 with the 64 KB ring alone, 2 with 16 KB of x
   const int64_t slots = int64_t(sm_count) * (has_x ? 2 : 3);
   TmaPlan p;
   const int64_t coltiles = cdiv(N, BC);
   int64_t split = slots / coltiles;
-  const int64_t min_split = has_x ? cdiv(M, kColsXRows) : 1;
+  const int64_t min_split = has_x ? cdiv(M, kColsXBytes / elem_bytes) : 1;
   const int64_t max_split = cdiv(M, 4 * BR);
   if (split > max_split) split = max_split;
   if (split < min_split) split = min_split;
@@ -446,8 +459,8 @@ inline TmaPlan plan_cols_tma(int64_t M, int64_t N, int sm_count, int elem_bytes,
   int64_t ctiles = cdiv(coltiles * p.split, slots);
   if (ctiles < 1) ctiles = 1;
   if (ctiles > 64) ctiles = 64;
-  p.ctiles = int(ctiles);
   p.tiles = cdiv(coltiles, ctiles);
+  p.full_wave = false;  // early launch (PDL) of a partial wave lands unevenly: measured slower
   return p;
 }
 
@@ -482,9 +495,10 @@ inline bool try_rows_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
     return true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));
-  rows_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(map, pol, M, N, xb, incx, p.per_split,
-                                                                     partials, h->tickets, h->dev_error);
-  *st = after_launch("rows_sweep_tma");
+  const cudaError_t le = launch_pdl(p.full_wave, rows_sweep_tma<P, T, HAS_X>, grid, dim3(kStThreads), smem,
+                                    h->stream, map, pol, M, N, xb, incx, p.per_split, partials, h->tickets,
+                                    h->dev_error);
+  *st = le != cudaSuccess ? cuda_fail(le, "rows_sweep_tma") : after_launch("rows_sweep_tma");
   return true;
 }
 
@@ -496,7 +510,7 @@ inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
   constexpr int BC = kStTileBytes / 1024;
   if (M < 4 * BR || N < BC) return false;
   TmaPlan p = plan_cols_tma(M, N, h->sm_count, sizeof(T), HAS_X);
-  if (p.split > 65535 || cdiv(N, BC) > int64_t(kMaxTickets) || p.tiles > INT32_MAX) return false;
+  if (p.tiles < 1 || p.split > 65535 || cdiv(N, BC) > int64_t(kMaxTickets) || p.tiles > INT32_MAX) return false;
   CUtensorMap map;
   if (!make_matrix_map(&map, A, M, N, lda, BR, BC)) return false;
   Acc* partials = nullptr;
@@ -509,15 +523,17 @@ inline bool try_cols_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
   const size_t smem = cols_tma_smem<T>(HAS_X, p.per_split);
   static std::atomic<uint64_t> attr{0};
   const cudaError_t ae = raise_smem_limit(attr, reinterpret_cast<const void*>(cols_sweep_tma<P, T, HAS_X>),
-                                          int(cols_tma_smem<T>(HAS_X, kColsXRows)), h->device);
+                                          int(cols_tma_smem<T>(HAS_X, kColsXBytes / int64_t(sizeof(T)))),
+                                          h->device);
   if (ae != cudaSuccess) {
     *st = cuda_fail(ae, "cols_sweep_tma: shared-memory limit");
     return true;
   }
   dim3 grid(unsigned(p.tiles), unsigned(p.split));
-  cols_sweep_tma<P, T, HAS_X><<<grid, kStThreads, smem, h->stream>>>(
-      map, pol, M, N, xb, incx, p.per_split, p.ctiles, partials, h->tickets, h->dev_error);
-  *st = after_launch("cols_sweep_tma");
+  const cudaError_t le = launch_pdl(p.full_wave, cols_sweep_tma<P, T, HAS_X>, grid, dim3(kStThreads), smem,
+                                    h->stream, map, pol, M, N, xb, incx, p.per_split, partials, h->tickets,
+                                    h->dev_error);
+  *st = le != cudaSuccess ? cuda_fail(le, "cols_sweep_tma") : after_launch("cols_sweep_tma");
   return true;
 }
 
