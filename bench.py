@@ -706,53 +706,45 @@ def grouped_error(torch, probs):
     return worst
 
 
-def bench_selector(torch, blas, sb, dev, shapes=48):
-    """Learned-selector spot check: regret of the learned selector and of the
-    size heuristic against exhaustive timing on fresh seeded shapes (the full
-    1000-shape held-out evaluation is in tuning/sgemm_selector_report.json)."""
+def bench_selector(torch, blas, sb, dev, n32=200, n64=50):
+    """Learned tile selector, measured live: on fresh seeded shapes (seeds
+    not in the training sweep; FP32 and FP64, the sweep's distributions and
+    caps) every config of the shape's element type is timed exhaustively and
+    the regret t(pick)/t(best) - 1 of the learned selector and of the size
+    heuristic is averaged per element type.  The held-out figures of the
+    training run (tuning/gemm_selector_report.json) are reported beside."""
     import ctypes as C
     from portblas_gb300 import _lib
     from portblas_gb300.tuning import sweep
     L = _lib.load()
-    rep_path = os.path.join(ROOT, "portblas_gb300", "tuning", "sgemm_selector_report.json")
+    rep_path = os.path.join(ROOT, "portblas_gb300", "tuning", "gemm_selector_report.json")
     report = json.load(open(rep_path)) if os.path.exists(rep_path) else None
-    ss = sweep.sample_shapes(shapes, seed=987654)
-    A = torch.rand(sweep.ELEM_CAP + 4096, device=dev)
-    B = torch.rand(sweep.ELEM_CAP + 4096, device=dev)
-    Cm = torch.zeros(sweep.ELEM_CAP + 65536, device=dev)
+    R = sweep.Runner(L, sb, torch, 987654, sweep.ELEM_CAP + 4096)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    r_mlp, r_heur = [], []
-    for s in ss:
-        m, n, k, bt = s["m"], s["n"], s["k"], s["batch"]
-        sa = (m * s["lda"]) if s["ta"] else (k * s["lda"])
-        sbs = (k * s["ldb"]) if s["tb"] else (n * s["ldb"])
-        sc = n * s["ldc"]
-        bt = max(1, min(bt, (sweep.ELEM_CAP + 4096) // max(sa, sbs, sc)))
-        ta, tb = (b"t" if s["ta"] else b"n"), (b"t" if s["tb"] else b"n")
-        t = np.full(40, np.inf)
-        for c in range(40):
-            run = lambda: L.gbblas_sgemm_strided_batched_config(sb.handle, c, ta, tb, m, n, k, 1.0, A.data_ptr(),
-                                                                s["lda"], sa, B.data_ptr(), s["ldb"], sbs, 0.0,
-                                                                Cm.data_ptr(), s["ldc"], sc, bt)
-            if run() != 0:
+    out = {}
+    for dt, count, seed in (("f32", n32, 987654), ("f64", n64, 987655)):
+        r_mlp, r_heur = [], []
+        for s in sweep.sample_shapes(count, seed=seed, dtype=dt):
+            t = R.time_all(s, e0, e1, min_ms=0.1, max_reps=5)
+            if not np.isfinite(t).any():
                 continue
-            e0.record()
-            for _ in range(3):
-                run()
-            e1.record()
-            e1.synchronize()
-            t[c] = e0.elapsed_time(e1) / 3
-        pick = C.c_int()
-        L.gbblas_sgemm_selector_pick(m, n, k, ta, tb, s["lda"], s["ldb"], s["ldc"], bt, C.byref(pick))
-        h = L.gbblas_sgemm_heuristic_config(m, n, k, bt)
-        r_mlp.append(t[pick.value] / t.min() - 1)
-        r_heur.append(t[h] / t.min() - 1)
-    out = {"live_shapes": shapes, "live_regret_mean": {"mlp": float(np.mean(r_mlp)),
-                                                       "heuristic": float(np.mean(r_heur))}}
+            code = sweep.DTYPE_F64 if dt == "f64" else sweep.DTYPE_F32
+            pick = C.c_int()
+            L.gbblas_gemm_selector_pick(code, s["m"], s["n"], s["k"], b"t" if s["ta"] else b"n",
+                                        b"t" if s["tb"] else b"n", s["lda"], s["ldb"], s["ldc"], s["batch"],
+                                        C.byref(pick))
+            h = L.gbblas_gemm_heuristic_config(code, s["m"], s["n"], s["k"], s["batch"])
+            r_mlp.append(t[pick.value] / t.min() - 1)
+            r_heur.append(t[h] / t.min() - 1)
+        out[dt] = {"live_shapes": len(r_mlp), "regret_mean": {"mlp": float(np.mean(r_mlp)),
+                                                              "heuristic": float(np.mean(r_heur))},
+                   "regret_median_mlp": float(np.median(r_mlp))}
+    res = {"live": out}
     if report:
-        out["heldout"] = {k: report[k] for k in ("heldout_shapes", "regret_mean", "total_time_over_exhaustive",
-                                                 "train_seconds") if k in report}
-    return out
+        res["heldout_training_run"] = {
+            "shapes": report.get("heldout_shapes"), "regret_mean": report.get("regret_mean"),
+            "per_dtype": {k: v and v["regret_mean"] for k, v in report.get("per_dtype", {}).items()}}
+    return res
 
 
 def summarize(c1, sg, bat, sel, pk) -> dict | None:
@@ -789,9 +781,8 @@ def summarize(c1, sg, bat, sel, pk) -> dict | None:
         out["strided4096x64"] = {"ms": r3(st["ms"]), "gbs": r3(st["gbs"]), "hbm_frac": r3(st["gbs"] / pk["hbm_gbs"]),
                                  "err": r3(st["max_norm_err_vs_fp64"])}
     if sel:
-        out["selector_regret"] = {"live": r3(sel["live_regret_mean"]["mlp"]), "live_shapes": sel["live_shapes"]}
-        if "heldout" in sel:
-            out["selector_regret"]["heldout"] = r3(sel["heldout"]["regret_mean"]["mlp"])
+        out["selector_regret_live"] = {dt: {"mlp": r3(v["regret_mean"]["mlp"]), "heuristic": r3(v["regret_mean"]["heuristic"]),
+                                            "shapes": v["live_shapes"]} for dt, v in sel["live"].items()}
     return out
 
 

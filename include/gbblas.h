@@ -255,14 +255,19 @@ gbblas_status_t gbblas_dsymm(gbblas_handle_t h, char side, char uplo, int64_t m,
                              const double* a, int64_t lda, const double* b, int64_t ldb, double beta, double* c,
                              int64_t ldc);
 
-/* FP32 GEMM tile configurations (no portBLAS counterpart: portBLAS fixes its
- * tile at compile time from size thresholds,
- * src/interface/blas3/backend/nvidia_gpu.hpp:116-171).  Configs 0..19 are
- * SIMT tiles {128x128, 128x64, 64x128, 64x64} x split-K {1,2,4,8,16};
- * 20..39 are the 3-term split-BF16 tcgen05 kernel with N tile {128, 64} x
- * split-K {1,2,4,8,16} x raster {N, M}.  All are FP32-accurate; AUTO picks
- * one per call (autotuned winner > learned selector > size heuristic). */
+/* GEMM tile configurations (no portBLAS counterpart: portBLAS fixes its
+ * tile at compile time from size thresholds per element type,
+ * src/interface/blas3/backend/nvidia_gpu.hpp:116-171).  FP32: configs 0..19
+ * are SIMT tiles {128x128, 128x64, 64x128, 64x64} x split-K {1,2,4,8,16},
+ * 20..39 the 3-term split-BF16 tcgen05 kernel with N tile {128, 64} x
+ * split-K {1,2,4,8,16} x raster {N, M}; all are FP32-accurate.  FP64:
+ * configs 40..59 are SIMT tiles x split-K as 0..19.  AUTO picks one of the
+ * element type's configs per call (autotuned winner > learned selector >
+ * size heuristic).  config_info takes any config (method 0 FP32 SIMT,
+ * 1 split-BF16, 2 FP64 SIMT); sgemm_config_count is 40 (FP32), gemm_config_
+ * count 60 (all). */
 int gbblas_sgemm_config_count(void);
+int gbblas_gemm_config_count(void);
 gbblas_status_t gbblas_sgemm_config_info(int config, int* method, int* tile_m, int* tile_n, int* split,
                                          int* raster_m);
 gbblas_status_t gbblas_sgemm_strided_batched_config(gbblas_handle_t h, int config, char transa, char transb,
@@ -270,21 +275,37 @@ gbblas_status_t gbblas_sgemm_strided_batched_config(gbblas_handle_t h, int confi
                                                     int64_t lda, int64_t stride_a, const float* b, int64_t ldb,
                                                     int64_t stride_b, float beta, float* c, int64_t ldc,
                                                     int64_t stride_c, int64_t batch_size);
+gbblas_status_t gbblas_dgemm_strided_batched_config(gbblas_handle_t h, int config, char transa, char transb,
+                                                    int64_t m, int64_t n, int64_t k, double alpha, const double* a,
+                                                    int64_t lda, int64_t stride_a, const double* b, int64_t ldb,
+                                                    int64_t stride_b, double beta, double* c, int64_t ldc,
+                                                    int64_t stride_c, int64_t batch_size);
 /* Selector inputs: log2 M, N, K (/14), transa, transb, lda/ldb/ldc mod 16
- * (/16), log2 batch (/10), dtype one-hot (FP32, BF16) — 11 floats. */
+ * (/16), log2 batch (/10), element type one-hot (FP32, FP64) — 11 floats.
+ * dtype is GBBLAS_DTYPE_F32 or GBBLAS_DTYPE_F64; the sgemm_ forms are FP32. */
+gbblas_status_t gbblas_gemm_features(int dtype, int64_t m, int64_t n, int64_t k, char transa, char transb,
+                                     int64_t lda, int64_t ldb, int64_t ldc, int64_t batch, float* features);
 gbblas_status_t gbblas_sgemm_features(int64_t m, int64_t n, int64_t k, char transa, char transb, int64_t lda,
                                       int64_t ldb, int64_t ldc, int64_t batch, float* features);
 /* The fixed size-threshold selector alone (portBLAS-style tiers). */
+int gbblas_gemm_heuristic_config(int dtype, int64_t m, int64_t n, int64_t k, int64_t batch);
 int gbblas_sgemm_heuristic_config(int64_t m, int64_t n, int64_t k, int64_t batch);
 /* Loads learned-selector weights (process-wide; default file
- * tuning/sgemm_selector.bin beside the package, or $GBBLAS_SGEMM_SELECTOR,
- * "off" disables), and asks the selector chain for a config. */
+ * tuning/gemm_selector.bin beside the package, or $GBBLAS_SGEMM_SELECTOR,
+ * "off" disables), and asks the selector chain for a config of the element
+ * type. */
 gbblas_status_t gbblas_sgemm_load_selector(const char* path);
+gbblas_status_t gbblas_gemm_selector_pick(int dtype, int64_t m, int64_t n, int64_t k, char transa, char transb,
+                                          int64_t lda, int64_t ldb, int64_t ldc, int64_t batch, int* config);
 gbblas_status_t gbblas_sgemm_selector_pick(int64_t m, int64_t n, int64_t k, char transa, char transb, int64_t lda,
                                            int64_t ldb, int64_t ldc, int64_t batch, int* config);
-/* Exhaustive autotune of one shape: times every config (`reps` launches
- * each) on zero-filled operands, remembers the winner for AUTO. */
+/* Exhaustive autotune of one shape: times every config of the element type
+ * (`reps` launches each) on zero-filled operands, remembers the winner for
+ * AUTO. */
 gbblas_status_t gbblas_sgemm_autotune(gbblas_handle_t h, char transa, char transb, int64_t m, int64_t n,
+                                      int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t batch, int reps,
+                                      int* best_config, float* best_ms);
+gbblas_status_t gbblas_dgemm_autotune(gbblas_handle_t h, char transa, char transb, int64_t m, int64_t n,
                                       int64_t k, int64_t lda, int64_t ldb, int64_t ldc, int64_t batch, int reps,
                                       int* best_config, float* best_ms);
 

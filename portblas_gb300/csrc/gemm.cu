@@ -46,7 +46,13 @@ static gbblas_status_t gemm_front(gbblas_handle_t h, char transa, char transb, i
   return dispatch_gemm(h, g);
 }
 
-gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<double>& g) { return launch_gemm_simt(h, g); }
+// FP64: the selector's pick among the FP64 SIMT configs (tile x split-K)
+gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<double>& g) {
+  gbblas_status_t s = launch_dgemm_config(h, g, select_dgemm_config(h, g));
+  if (s != GBBLAS_STATUS_UNSUPPORTED) return s;
+  clear_error();  // a config that cannot take this shape (grid / workspace limits)
+  return launch_gemm_simt(h, g);
+}
 
 gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g) {
   switch (h->sgemm_mode) {

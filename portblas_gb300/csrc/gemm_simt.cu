@@ -17,6 +17,9 @@ gbblas_status_t launch_simt_tile_128x64(gbblas_handle_t h, const GemmArgs<float>
 gbblas_status_t launch_simt_tile_64x128(gbblas_handle_t h, const GemmArgs<float>& g, int split);
 gbblas_status_t launch_simt_tile_64x64(gbblas_handle_t h, const GemmArgs<float>& g, int split);
 gbblas_status_t launch_simt_tile_128x128_f64(gbblas_handle_t h, const GemmArgs<double>& g, int split);
+gbblas_status_t launch_simt_tile_128x64_f64(gbblas_handle_t h, const GemmArgs<double>& g, int split);
+gbblas_status_t launch_simt_tile_64x128_f64(gbblas_handle_t h, const GemmArgs<double>& g, int split);
+gbblas_status_t launch_simt_tile_64x64_f64(gbblas_handle_t h, const GemmArgs<double>& g, int split);
 
 gbblas_status_t launch_gemm_simt_tiled(gbblas_handle_t h, const GemmArgs<float>& g, int tile, int split) {
   switch (tile) {
@@ -24,6 +27,16 @@ gbblas_status_t launch_gemm_simt_tiled(gbblas_handle_t h, const GemmArgs<float>&
     case kSimtTile128x64: return launch_simt_tile_128x64(h, g, split);
     case kSimtTile64x128: return launch_simt_tile_64x128(h, g, split);
     case kSimtTile64x64: return launch_simt_tile_64x64(h, g, split);
+  }
+  return fail(GBBLAS_STATUS_INVALID_ARG, "gemm: unknown SIMT tile");
+}
+
+gbblas_status_t launch_gemm_simt_tiled(gbblas_handle_t h, const GemmArgs<double>& g, int tile, int split) {
+  switch (tile) {
+    case kSimtTile128x128: return launch_simt_tile_128x128_f64(h, g, split);
+    case kSimtTile128x64: return launch_simt_tile_128x64_f64(h, g, split);
+    case kSimtTile64x128: return launch_simt_tile_64x128_f64(h, g, split);
+    case kSimtTile64x64: return launch_simt_tile_64x64_f64(h, g, split);
   }
   return fail(GBBLAS_STATUS_INVALID_ARG, "gemm: unknown SIMT tile");
 }

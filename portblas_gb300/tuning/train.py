@@ -1,15 +1,17 @@
-"""Trains the FP32 GEMM tile selector on a sweep's timing table with the
+"""Trains the GEMM tile selector on a sweep's timing table with the
 library's own CUDA kernels (gbblas_mlp_loss_grad / gbblas_mlp_adam), then
-measures its regret against exhaustive autotuning on held-out shapes.
+measures its regret against exhaustive autotuning on held-out shapes, per
+element type.
 
 Target: for each shape and config, log2(t_config / t_best), clipped at 8
-(configs that cannot run are masked out).  Selection = argmin of the
-predicted targets.  Regret of a selector on a shape = t(pick)/t(best) - 1.
+(configs that cannot run, or belong to the other element type, are masked
+out).  Selection = argmin of the predicted targets over the shape's element
+type's configs.  Regret of a selector on a shape = t(pick)/t(best) - 1.
 
 Run on a GPU:
   python -m portblas_gb300.tuning.train --sweep FILE.npz --out-dir DIR
-writes DIR/sgemm_selector.bin (the weights the library loads) and
-DIR/sgemm_selector_report.json.
+writes DIR/gemm_selector.bin (the weights the library loads) and
+DIR/gemm_selector_report.json.
 """
 from __future__ import annotations
 
@@ -22,7 +24,8 @@ import time
 
 import numpy as np
 
-IN, HID, OUT = 11, 64, 40
+IN, HID, OUT = 11, 64, 60
+F64_FIRST = 40  # FP32 configs [0, 40), FP64 configs [40, 60)
 CLIP = 8.0
 
 
@@ -77,6 +80,7 @@ def main():
     T = d["times_ms"].astype(np.float64)
     keep = np.isfinite(T).any(axis=1)
     X, T, shapes = X[keep], T[keep], d["shapes"][keep]
+    dt = d["dtype"][keep] if "dtype" in d.files else np.zeros(len(X), np.int8)
     Y, Mk = targets(T)
     ntr = min(args.train, len(X) - 1)
     Xtr, Ytr, Mtr = X[:ntr], Y[:ntr], Mk[:ntr]
@@ -118,34 +122,58 @@ def main():
         assert st == 0, L.gbblas_last_error()
         return ys.cpu().numpy()
 
-    pick_mlp = predict(Xte).argmin(1)
-    pick_heur = np.array([L.gbblas_sgemm_heuristic_config(int(s[0]), int(s[1]), int(s[2]), int(s[3]))
-                          for s in shapes[ntr:]])
-    # best single fixed config (chosen on the training shapes)
-    fixed = int(np.argmin(Ytr.mean(0)))  # mean clipped log2 slowdown over the training shapes
-    pick_fixed = np.full(len(Xte), fixed)
+    def pick_in_range(pred, is64):
+        lo = np.where(is64, F64_FIRST, 0)
+        hi = np.where(is64, OUT, F64_FIRST)
+        col = np.arange(OUT)[None, :]
+        masked = np.where((col >= lo[:, None]) & (col < hi[:, None]), pred, np.inf)
+        return masked.argmin(1)
+
+    is64_tr, is64_te = dt[:ntr] == 1, dt[ntr:] == 1
+    pick_mlp = pick_in_range(predict(Xte), is64_te)
+    pick_heur = np.array([L.gbblas_gemm_heuristic_config(2 if f64 else 0, int(s[0]), int(s[1]), int(s[2]),
+                                                         int(s[3]))
+                          for s, f64 in zip(shapes[ntr:], is64_te)])
+    # best single fixed config per element type (chosen on the training shapes)
+    fixed = {}
+    for name, sel, lo, hi in (("f32", ~is64_tr, 0, F64_FIRST), ("f64", is64_tr, F64_FIRST, OUT)):
+        fixed[name] = lo + int(np.argmin(Ytr[sel][:, lo:hi].mean(0))) if sel.any() else lo
+    pick_fixed = np.where(is64_te, fixed["f64"], fixed["f32"])
     r_mlp, r_heur, r_fix = regret(Tte, pick_mlp), regret(Tte, pick_heur), regret(Tte, pick_fixed)
-    tot_best = float(Tte.min(1).sum())
+
+    def summary(sel):
+        if not sel.any():
+            return None
+        tb = float(Tte[sel].min(1).sum())
+        idx = np.flatnonzero(sel)
+        return {
+            "heldout_shapes": int(sel.sum()),
+            "regret_mean": {"mlp": float(r_mlp[sel].mean()), "heuristic": float(r_heur[sel].mean()),
+                            "best_fixed_config": float(r_fix[sel].mean())},
+            "regret_median": {"mlp": float(np.median(r_mlp[sel])), "heuristic": float(np.median(r_heur[sel]))},
+            "regret_p90": {"mlp": float(np.quantile(r_mlp[sel], 0.9)),
+                           "heuristic": float(np.quantile(r_heur[sel], 0.9))},
+            "total_time_over_exhaustive": {"mlp": float(Tte[idx, pick_mlp[sel]].sum() / tb),
+                                           "heuristic": float(Tte[idx, pick_heur[sel]].sum() / tb)},
+            "exact_pick_rate_mlp": float((pick_mlp[sel] == Tte[sel].argmin(1)).mean()),
+        }
+
+    all_te = np.ones(len(Xte), dtype=bool)
     report = {
-        "train_shapes": int(ntr), "heldout_shapes": int(len(Xte)), "configs": OUT, "hidden": HID,
+        "train_shapes": int(ntr), "configs": OUT, "hidden": HID,
         "steps": args.steps, "batch": args.batch, "train_seconds": train_s, "loss_history": hist,
-        "regret_mean": {"mlp": float(r_mlp.mean()), "heuristic": float(r_heur.mean()),
-                        "best_fixed_config": float(r_fix.mean())},
-        "regret_median": {"mlp": float(np.median(r_mlp)), "heuristic": float(np.median(r_heur))},
-        "regret_p90": {"mlp": float(np.quantile(r_mlp, 0.9)), "heuristic": float(np.quantile(r_heur, 0.9))},
-        "total_time_over_exhaustive": {
-            "mlp": float(Tte[np.arange(len(Xte)), pick_mlp].sum() / tot_best),
-            "heuristic": float(Tte[np.arange(len(Xte)), pick_heur].sum() / tot_best)},
-        "exact_pick_rate_mlp": float((pick_mlp == Tte.argmin(1)).mean()),
+        **summary(all_te),
+        "per_dtype": {"f32": summary(~is64_te), "f64": summary(is64_te)},
         "best_fixed_config": fixed,
         "sweep_meta": json.loads(str(d["meta"])),
     }
     os.makedirs(args.out_dir, exist_ok=True)
     params = P.cpu().numpy()
-    write_bin(os.path.join(args.out_dir, "sgemm_selector.bin"), params)
-    with open(os.path.join(args.out_dir, "sgemm_selector_report.json"), "w") as f:
+    write_bin(os.path.join(args.out_dir, "gemm_selector.bin"), params)
+    with open(os.path.join(args.out_dir, "gemm_selector_report.json"), "w") as f:
         json.dump(report, f, indent=1)
-    print(json.dumps(report["regret_mean"]), json.dumps(report["total_time_over_exhaustive"]))
+    print(json.dumps(report["regret_mean"]), json.dumps(report["total_time_over_exhaustive"]),
+          json.dumps({k: v and v["regret_mean"] for k, v in report["per_dtype"].items()}))
 
 
 if __name__ == "__main__":

@@ -61,3 +61,49 @@ def test_autotune_and_auto_use_winner(sb, torch_cuda):
     pick = C.c_int()
     assert L.gbblas_sgemm_selector_pick(96, 80, 512, b"n", b"n", 96, 512, 96, 1, C.byref(pick)) == 0
     assert pick.value == best.value
+
+
+@pytest.mark.parametrize("cfg", range(40, 60))
+def test_every_fp64_config(sb, torch_cuda, cfg):
+    """The FP64 configs (SIMT tiles x split-K) against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import _lib
+    L = _lib.load()
+    for (m, n, k, batch, ta, tb) in SHAPES:
+        g = rng(m + n + k + batch + cfg)
+        lda, ldb, ldc = (k if ta else m) + 1, (n if tb else k) + 2, m + 3
+        sa, sbs, sc = lda * (m if ta else k), ldb * (k if tb else n), ldc * n
+        a = g.uniform(-1, 1, sa * batch)
+        b = g.uniform(-1, 1, sbs * batch)
+        c = g.uniform(-1, 1, sc * batch)
+        cd = torch.from_numpy(c.copy()).cuda()
+        ad, bd = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        st = L.gbblas_dgemm_strided_batched_config(sb.handle, cfg, b"t" if ta else b"n", b"t" if tb else b"n", m,
+                                                   n, k, 1.5, ad.data_ptr(), lda, sa, bd.data_ptr(), ldb, sbs, 0.5,
+                                                   cd.data_ptr(), ldc, sc, batch)
+        assert st == 0, (cfg, m, n, k, L.gbblas_last_error())
+        out = cd.cpu().numpy()
+        for i in range(batch):
+            ref = oracle.gemm(ta, tb, m, n, k, 1.5, a[i * sa:], lda, b[i * sbs:], ldb, 0.5, c[i * sc:], ldc)
+            got = out[i * sc:(i + 1) * sc].reshape(n, ldc).T[:m]
+            assert_almost_equal(got, ref, dtype=np.float64)
+            np.testing.assert_array_equal(out[i * sc:(i + 1) * sc].reshape(n, ldc).T[m:],
+                                          c[i * sc:(i + 1) * sc].reshape(n, ldc).T[m:])
+    # FP32 entry points refuse FP64 configs and the other way round
+    buf = torch.zeros(16, device="cuda", dtype=torch.float64)
+    assert L.gbblas_dgemm_strided_batched_config(sb.handle, 3, b"n", b"n", 2, 2, 2, 1.0, buf.data_ptr(), 2, 4,
+                                                 buf.data_ptr(), 2, 4, 0.0, buf.data_ptr(), 2, 4, 1) == 1
+    sb.check_device_error()
+
+
+def test_dgemm_autotune_and_auto_use_winner(sb, torch_cuda):
+    import ctypes as C
+    from portblas_gb300 import _lib
+    L = _lib.load()
+    best, ms = C.c_int(), C.c_float()
+    assert L.gbblas_dgemm_autotune(sb.handle, b"t", b"n", 96, 80, 512, 512, 512, 96, 1, 2, C.byref(best),
+                                   C.byref(ms)) == 0
+    assert 40 <= best.value < 60 and ms.value > 0
+    pick = C.c_int()
+    assert L.gbblas_gemm_selector_pick(2, 96, 80, 512, b"t", b"n", 512, 512, 96, 1, C.byref(pick)) == 0
+    assert pick.value == best.value

@@ -9,7 +9,7 @@ import pytest
 from oracle import mlp as omlp
 
 pytestmark = pytest.mark.gpu
-IN, HID, OUT = 11, 64, 40
+IN, HID, OUT = 11, 64, 60
 
 
 @pytest.fixture(scope="module")
