@@ -139,20 +139,25 @@ __global__ void __launch_bounds__(256, 6) gemm_small_batched_kernel(GemmArgs<flo
     }
 }
 
-// ------------------------------------------- small batches, pipelined --
+// ------------------------------------------- small batches, 8 x 8 tiles --
 // The 16-byte-aligned case (M, N, K multiples of 4, leading dimensions and
-// strides multiples of 4 floats): persistent CTAs walk the batch and copy
-// problem p+1's A and B into the second of two shared buffers with
-// cp.async while they compute problem p, so loads and FMAs overlap inside
-// every CTA.  Operands keep their memory layout in shared memory (64 rows of
+// strides multiples of 4 floats): persistent 64-thread CTAs, six per SM,
+// walk the batch one problem at a time.  A CTA copies the problem's A and B
+// into shared memory with 16-byte cp.async (memory layout kept: 64 rows of
 // 64 floats; rows whose k is contiguous have their 16-byte chunks XOR-
-// swizzled by row / 4 so the per-thread 128-bit reads hit distinct banks);
-// the inner loop takes 4 k at a time as 4 + 4 128-bit reads for 64 FMAs.
-constexpr int kPipeRow = 64;                         // floats per shared row
-constexpr int kPipeTile = kSmallMax * kPipeRow;      // floats per operand buffer
-constexpr int kPipeCtasPerSm = 3;                    // 64 KB of buffers each
+// swizzled by row / 8), then each thread computes an 8 x 8 block of C from
+// 128-bit shared reads: 4 k at a time, 8 + 8 reads feed 256 FMAs, and every
+// read of a warp is conflict-free (its rows share one swizzle key per
+// thread and differ across threads).  While one CTA computes, the others on
+// its SM wait on their copies, so the copies and the FMAs overlap.  (Six
+// single-buffered CTAs measured faster than three double-buffered ones:
+// 64.5 against 75.6 us for 4096 x 64^3; the earlier 4 x 4 tiles ran 73 us.)
+constexpr int kR8Threads = 64;
+constexpr int kR8CtasPerSm = 6;
+constexpr int kR8Row = 64;                          // floats per shared row
+constexpr int kR8Tile = kSmallMax * kR8Row;         // floats per operand
 
-__device__ __forceinline__ int pipe_swz(int row, int chunk) { return (chunk ^ ((row >> 2) & 7)) * 4; }
+__device__ __forceinline__ int r8_swz(int row, int chunk) { return (chunk ^ ((row >> 3) & 7)) * 4; }
 
 __device__ __forceinline__ void cp_async16(float* dst, const float* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
@@ -164,109 +169,105 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // rows x cols floats of X (row r at X + r*ld, cols contiguous) into S;
-// SWZ: chunk c of row r goes to chunk c ^ ((r / 4) % 8)
+// SWZ: chunk c of row r goes to chunk c ^ ((r / 8) % 8)
 template <bool SWZ>
-__device__ __forceinline__ void pipe_copy(float* S, const float* X, int64_t ld, int rows, int cols, int t) {
+__device__ __forceinline__ void r8_copy(float* S, const float* X, int64_t ld, int rows, int cols, int t) {
   const int cpr = cols >> 2;  // chunks per row
-  for (int e = t; e < rows * 16; e += 256) {
+  for (int e = t; e < rows * 16; e += kR8Threads) {
     const int r = e >> 4, c = e & 15;
-    if (c < cpr) cp_async16(S + r * kPipeRow + (SWZ ? pipe_swz(r, c) : 4 * c), X + int64_t(r) * ld + 4 * c);
+    if (c < cpr) cp_async16(S + r * kR8Row + (SWZ ? r8_swz(r, c) : 4 * c), X + int64_t(r) * ld + 4 * c);
   }
 }
 
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(256, kPipeCtasPerSm) gemm_small_batched_pipe_kernel(GemmArgs<float> g) {
-  extern __shared__ __align__(16) float pipe_smem[];  // [2][A, B][kPipeTile]
+__global__ void __launch_bounds__(kR8Threads, kR8CtasPerSm) gemm_small_batched_r8_kernel(GemmArgs<float> g) {
+  extern __shared__ __align__(16) float r8_smem[];  // [A, B][kR8Tile]
+  float* SA = r8_smem;
+  float* SB = r8_smem + kR8Tile;
   const int M = int(g.m), N = int(g.n), K = int(g.k), t = threadIdx.x;
-  const int tx = t % 16, ty = t / 16;
+  const int tx = t & 7, ty = t >> 3;  // C rows 8ty .. 8ty+7, columns 8tx .. 8tx+7
   // A(i, k): TA ? rows i, k contiguous (swizzled) : rows k, i contiguous
   // B(k, j): TB ? rows k, j contiguous : rows j, k contiguous (swizzled)
-  auto issue = [&](int64_t p, int buf) {
-    float* SA = pipe_smem + buf * 2 * kPipeTile;
-    float* SB = SA + kPipeTile;
+  for (int64_t p = blockIdx.x; p < g.batch; p += gridDim.x) {
     const float* A = g.a + p * g.stride_a;
     const float* B = g.b + p * g.stride_b;
-    if (TA) pipe_copy<true>(SA, A, g.lda, M, K, t);
-    else pipe_copy<false>(SA, A, g.lda, K, M, t);
-    if (TB) pipe_copy<false>(SB, B, g.ldb, K, N, t);
-    else pipe_copy<true>(SB, B, g.ldb, N, K, t);
+    if (TA) r8_copy<true>(SA, A, g.lda, M, K, t);
+    else r8_copy<false>(SA, A, g.lda, K, M, t);
+    if (TB) r8_copy<false>(SB, B, g.ldb, K, N, t);
+    else r8_copy<true>(SB, B, g.ldb, N, K, t);
     cp_async_commit();
-  };
-  int64_t p = blockIdx.x;
-  if (p < g.batch) issue(p, 0);
-  for (int buf = 0; p < g.batch; p += gridDim.x, buf ^= 1) {
-    const int64_t pn = p + gridDim.x;
-    if (pn < g.batch) {
-      issue(pn, buf ^ 1);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
+    cp_async_wait<0>();
     __syncthreads();
-    const float* SA = pipe_smem + buf * 2 * kPipeTile;
-    const float* SB = SA + kPipeTile;
-    float acc[4][4] = {};
-    // swizzled operands: this thread's rows 4ty.. / 4tx.. share one XOR key
-    const float* ra = SA + (TA ? 4 * ty * kPipeRow : 4 * ty);
-    const float* rb = SB + (TB ? 4 * tx : 4 * tx * kPipeRow);
-    const int ka = ty & 7, kb = tx & 7;
-#pragma unroll 4
-    for (int k = 0; k < K; k += 4) {
-      float a[4][4], b[4][4];  // a[i][kk], b[kk][j]
-      const int oa = TA ? ((k >> 2) ^ ka) * 4 : k * kPipeRow;
-      const int ob = TB ? k * kPipeRow : ((k >> 2) ^ kb) * 4;
+    float acc[8][8];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (TA) {  // row 4ty+q, k..k+3
-          const float4 v = *reinterpret_cast<const float4*>(ra + q * kPipeRow + oa);
-          a[q][0] = v.x; a[q][1] = v.y; a[q][2] = v.z; a[q][3] = v.w;
-        } else {  // row k+q, i = 4ty..4ty+3
-          const float4 v = *reinterpret_cast<const float4*>(ra + q * kPipeRow + oa);
-          a[0][q] = v.x; a[1][q] = v.y; a[2][q] = v.z; a[3][q] = v.w;
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll 2
+    for (int k = 0; k < K; k += 4) {
+      float a[8][4], b[4][8];  // a[i][kk] = A(8ty+i, k+kk), b[kk][j] = B(k+kk, 8tx+j)
+      if (TA) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float4 v = *reinterpret_cast<const float4*>(SA + (8 * ty + i) * kR8Row + r8_swz(8 * ty, k >> 2));
+          a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
         }
-        if (TB) {  // row k+q, j = 4tx..4tx+3
-          const float4 v = *reinterpret_cast<const float4*>(rb + q * kPipeRow + ob);
-          b[q][0] = v.x; b[q][1] = v.y; b[q][2] = v.z; b[q][3] = v.w;
-        } else {  // row 4tx+q (column j), k..k+3
-          const float4 v = *reinterpret_cast<const float4*>(rb + q * kPipeRow + ob);
-          b[0][q] = v.x; b[1][q] = v.y; b[2][q] = v.z; b[3][q] = v.w;
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 v = *reinterpret_cast<const float4*>(SA + (k + kk) * kR8Row + 8 * ty + 4 * h);
+            a[4 * h][kk] = v.x; a[4 * h + 1][kk] = v.y; a[4 * h + 2][kk] = v.z; a[4 * h + 3][kk] = v.w;
+          }
+      }
+      if (TB) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 v = *reinterpret_cast<const float4*>(SB + (k + kk) * kR8Row + 8 * tx + 4 * h);
+            b[kk][4 * h] = v.x; b[kk][4 * h + 1] = v.y; b[kk][4 * h + 2] = v.z; b[kk][4 * h + 3] = v.w;
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float4 v = *reinterpret_cast<const float4*>(SB + (8 * tx + j) * kR8Row + r8_swz(8 * tx, k >> 2));
+          b[0][j] = v.x; b[1][j] = v.y; b[2][j] = v.z; b[3][j] = v.w;
         }
       }
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 8; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i][kk], b[kk][j], acc[i][j]);
+          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i][kk], b[kk][j], acc[i][j]);
     }
-    // C(i, j) for i = 4ty.., j = 4tx..: each column's 4 rows as one 128-bit access
+    __syncthreads();  // the operands of the next problem overwrite these buffers
+    // C(i, j), i = 8ty.., j = 8tx..: each column's 8 rows as two 128-bit
+    // accesses; a column's old values are loaded before its stores
     float* C = g.c + p * g.stride_c;
-    if (4 * ty < M) {
-      // the four columns of C are loaded before any store so the loads overlap
-      float4 o[4];
-      if (g.beta != 0.f) {
+    if (8 * ty < M) {
+      const bool two = 8 * ty + 4 < M;
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-          o[j] = (4 * tx + j < N) ? *reinterpret_cast<const float4*>(C + 4 * ty + int64_t(4 * tx + j) * g.ldc)
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int gj = 4 * tx + j;
-        if (gj < N) {
-          float4* cp = reinterpret_cast<float4*>(C + 4 * ty + int64_t(gj) * g.ldc);
-          float4 v = make_float4(g.alpha * acc[0][j], g.alpha * acc[1][j], g.alpha * acc[2][j], g.alpha * acc[3][j]);
-          if (g.beta != 0.f) {
-            v.x = fmaf(g.beta, o[j].x, v.x);
-            v.y = fmaf(g.beta, o[j].y, v.y);
-            v.z = fmaf(g.beta, o[j].z, v.z);
-            v.w = fmaf(g.beta, o[j].w, v.w);
-          }
-          *cp = v;
+      for (int j = 0; j < 8; ++j) {
+        const int gj = 8 * tx + j;
+        if (gj >= N) continue;
+        float4* cp = reinterpret_cast<float4*>(C + 8 * ty + int64_t(gj) * g.ldc);
+        float4 v0 = make_float4(g.alpha * acc[0][j], g.alpha * acc[1][j], g.alpha * acc[2][j], g.alpha * acc[3][j]);
+        float4 v1 = make_float4(g.alpha * acc[4][j], g.alpha * acc[5][j], g.alpha * acc[6][j], g.alpha * acc[7][j]);
+        if (g.beta != 0.f) {
+          const float4 o0 = cp[0];
+          const float4 o1 = two ? cp[1] : make_float4(0.f, 0.f, 0.f, 0.f);
+          v0.x = fmaf(g.beta, o0.x, v0.x); v0.y = fmaf(g.beta, o0.y, v0.y);
+          v0.z = fmaf(g.beta, o0.z, v0.z); v0.w = fmaf(g.beta, o0.w, v0.w);
+          v1.x = fmaf(g.beta, o1.x, v1.x); v1.y = fmaf(g.beta, o1.y, v1.y);
+          v1.z = fmaf(g.beta, o1.z, v1.z); v1.w = fmaf(g.beta, o1.w, v1.w);
         }
+        cp[0] = v0;
+        if (two) cp[1] = v1;
       }
     }
-    __syncthreads();  // this buffer is refilled by the next iteration's prefetch
   }
 }
 
@@ -284,22 +285,22 @@ bool small_batched_applies(const GemmArgs<float>& g, int sm_count) {
 
 gbblas_status_t launch_gemm_small_batched(gbblas_handle_t h, const GemmArgs<float>& g) {
   if (small_pipe_applies(g)) {
-    constexpr int smem = 4 * kPipeTile * int(sizeof(float));
-    const int64_t cap = int64_t(h->sm_count) * kPipeCtasPerSm;
+    constexpr int smem = 2 * kR8Tile * int(sizeof(float));
+    const int64_t cap = int64_t(h->sm_count) * kR8CtasPerSm;
     const unsigned grid = unsigned(g.batch < cap ? g.batch : cap);
-#define GB_PIPE(TA_, TB_)                                                                                    \
-  if (g.ta == TA_ && g.tb == TB_) {                                                                          \
-    static std::atomic<uint64_t> attr{0};                                                                    \
-    GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(gemm_small_batched_pipe_kernel<TA_, TB_>), \
-                                 smem, h->device));                                                          \
-    gemm_small_batched_pipe_kernel<TA_, TB_><<<grid, 256, smem, h->stream>>>(g);                             \
+#define GB_R8(TA_, TB_)                                                                                     \
+  if (g.ta == TA_ && g.tb == TB_) {                                                                         \
+    static std::atomic<uint64_t> attr{0};                                                                   \
+    GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(gemm_small_batched_r8_kernel<TA_, TB_>), \
+                                 smem, h->device));                                                         \
+    gemm_small_batched_r8_kernel<TA_, TB_><<<grid, kR8Threads, smem, h->stream>>>(g);                        \
   }
-    GB_PIPE(false, false)
-    GB_PIPE(false, true)
-    GB_PIPE(true, false)
-    GB_PIPE(true, true)
-#undef GB_PIPE
-    return after_launch("gemm_small_batched_pipe");
+    GB_R8(false, false)
+    GB_R8(false, true)
+    GB_R8(true, false)
+    GB_R8(true, true)
+#undef GB_R8
+    return after_launch("gemm_small_batched_r8");
   }
   const dim3 grid(unsigned(g.batch));
 #define GB_SMALL(TA_, TB_) \
