@@ -30,6 +30,9 @@ gbblas_status_t launch_gemm_interleaved(gbblas_handle_t h, const GemmArgs<double
 // one CTA per problem.
 bool small_batched_applies(const GemmArgs<float>& g, int sm_count);
 gbblas_status_t launch_gemm_small_batched(gbblas_handle_t h, const GemmArgs<float>& g);
+// The same batches (M, N, K <= 64) on the tcgen05 tensor cores, two problems
+// per tile; UNSUPPORTED (nothing launched) when TMA cannot address the layout.
+gbblas_status_t launch_gemm_small_batched_tc(gbblas_handle_t h, const GemmArgs<float>& g);
 // FP32 / FP64 SIMT GEMM with an explicit CTA tile and split-K factor.
 enum : int { kSimtTile128x128 = 0, kSimtTile128x64 = 1, kSimtTile64x128 = 2, kSimtTile64x64 = 3 };
 gbblas_status_t launch_gemm_simt_tiled(gbblas_handle_t h, const GemmArgs<float>& g, int tile, int split);

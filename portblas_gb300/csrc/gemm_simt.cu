@@ -284,6 +284,10 @@ bool small_batched_applies(const GemmArgs<float>& g, int sm_count) {
 }
 
 gbblas_status_t launch_gemm_small_batched(gbblas_handle_t h, const GemmArgs<float>& g) {
+  {
+    const gbblas_status_t s = launch_gemm_small_batched_tc(h, g);
+    if (s != GBBLAS_STATUS_UNSUPPORTED) return s;
+  }
   if (small_pipe_applies(g)) {
     constexpr int smem = 2 * kR8Tile * int(sizeof(float));
     const int64_t cap = int64_t(h->sm_count) * kR8CtasPerSm;

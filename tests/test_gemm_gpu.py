@@ -341,3 +341,35 @@ def test_gemm_tall_skinny_split_k(sb, torch_cuda, mode):
     err = np.abs(got[rows, cols] - ref) / scale
     assert err.max() <= 2.0 * (k + 4) * 2.0 ** -24, err.max()
     sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("m,n,k,beta", [(64, 64, 64, 0.0), (40, 24, 52, 0.5)])
+def test_gemm_strided_small_batch_tensor_cores(sb, torch_cuda, ta, tb, m, n, k, beta):
+    """The tensor-core small-batch path (16-byte-aligned layouts, two
+    problems per tile): an odd batch, so the last tile holds one problem and
+    a zero-filled one; every problem's C against FP64 at FP32-level accuracy
+    (|A||B|-normalised), the neighbouring padding of C untouched."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    g = rng(11 * m + 3 * n + k)
+    batch = 611
+    lda, ldb, ldc = (k if ta else m) + 4, (n if tb else k) + 8, m + 1
+    sa, sbs, sc = lda * (m if ta else k), ldb * (k if tb else n) + 4, ldc * n + 3
+    a = g.uniform(-1, 1, sa * batch).astype(np.float32)
+    b = g.uniform(-1, 1, sbs * batch).astype(np.float32)
+    c = g.uniform(-1, 1, sc * batch).astype(np.float32)
+    cd = to_dev(c, torch)
+    blas._gemm_strided_batched(sb, "t" if ta else "n", "t" if tb else "n", m, n, k, 1.5, to_dev(a, torch), lda, sa,
+                               to_dev(b, torch), ldb, sbs, beta, cd, ldc, sc, batch)
+    out = to_host(cd)
+    for i in (0, 1, 2, 305, batch - 2, batch - 1):
+        ref = oracle.gemm(ta, tb, m, n, k, 1.5, a[i * sa:], lda, b[i * sbs:], ldb, beta, c[i * sc:], ldc)
+        scale = oracle.gemm_absscale(ta, tb, m, n, k, 1.5, a[i * sa:], lda, b[i * sbs:], ldb, beta, c[i * sc:], ldc)
+        blk = out[i * sc:i * sc + ldc * n].reshape(n, ldc).T
+        got = blk[:m]
+        assert (np.abs(got - ref) / scale).max() <= 2.0 * (k + 2) * U32, i
+        np.testing.assert_array_equal(blk[m:], c[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:])
+        np.testing.assert_array_equal(out[i * sc + ldc * n:(i + 1) * sc], c[i * sc + ldc * n:(i + 1) * sc])
+    sb.check_device_error()
