@@ -594,7 +594,14 @@ def bench_batched(torch, blas, sb, dev, reps=10):
                               "max_norm_err_vs_fp64": grouped_error(torch, probs[::128])}
         plan.close()
         del probs
-    # strided batch 4096 x 64^3 FP32 (A, B, C 64 MiB each)
+    out["strided_4096x64"] = bench_strided(torch, blas, sb, dev, reps)
+    out["grouped_splitk"] = bench_grouped_splitk(torch, blas, sb, dev, reps)
+    return out
+
+
+def bench_strided(torch, blas, sb, dev, reps=10):
+    """Strided batch of 4096 FP32 problems of 64^3 (A, B, C 64 MiB each,
+    inputs U[0, 1)); error of three problems against FP64, |A||B|-normalised."""
     nb, n = 4096, 64
     A = torch.rand(nb * n * n, device=dev)
     B = torch.rand(nb * n * n, device=dev)
@@ -619,10 +626,8 @@ def bench_batched(torch, blas, sb, dev, reps=10):
         ref = Ai @ Bi
         scale = Ai.abs() @ Bi.abs()
         errs.append(float(((Cc[i * n * n:(i + 1) * n * n].view(n, n).T.double() - ref).abs() / scale).max().item()))
-    out["strided_4096x64"] = {"ms": ms, "tflops": f / (ms * 1e-3) / 1e12, "gbs": byt / (ms * 1e-3) / 1e9,
-                              "max_norm_err_vs_fp64": max(errs)}
-    out["grouped_splitk"] = bench_grouped_splitk(torch, blas, sb, dev, reps)
-    return out
+    return {"ms": ms, "tflops": f / (ms * 1e-3) / 1e12, "gbs": byt / (ms * 1e-3) / 1e9, "bytes_per_call": byt,
+            "max_norm_err_vs_fp64": max(errs)}
 
 
 SPLITK_CASES = {
@@ -849,7 +854,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-sgemm", action="store_true", help="skip the SGEMM/DGEMM set")
-    ap.add_argument("--profile", choices=["memory", "sgemm", "batched"], default=None,
+    ap.add_argument("--profile", choices=["memory", "sgemm", "batched", "strided"], default=None,
                     help="short run of one workload only (no e2e, CPU baseline or JSON line), for ncu captures")
     ap.add_argument("--sgemm-n", type=int, default=8192)
     args = ap.parse_args()
@@ -894,6 +899,9 @@ def main():
         return
     if args.profile == "batched":
         print(json.dumps({"profile": "batched", "res": bench_batched(torch, blas, sb, dev, reps=2)}))
+        return
+    if args.profile == "strided":
+        print(json.dumps({"profile": "strided", "res": bench_strided(torch, blas, sb, dev, reps=args.steps)}))
         return
     if args.profile == "sgemm":
         r = bench_sgemm(torch, blas, sb, dev, reps=1, n=args.sgemm_n, with_dgemm=False)
