@@ -27,6 +27,7 @@
 // or B, so the tensor-core kernel only ever sees K-major operands.
 #include <cuda_bf16.h>
 
+#include <cstdlib>
 #include <mutex>
 
 #include "gemm_internal.cuh"
@@ -283,6 +284,215 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+// ---------------------------------------------------- CTA-pair (2-SM) tiles --
+// The 2-term split (x3) on 256 x 128 output tiles, one per cluster of two
+// CTAs: each CTA loads its own 128 rows of A and half (64 rows) of the B
+// tile, so a stage is 48 KB instead of 64 and four fit; the even CTA's MMA
+// lane issues tcgen05.mma.cta_group::2 (M = 256: A rows 0..127 from the even
+// CTA, 128..255 from the odd one; B columns 0..63 from the even CTA, 64..127
+// from the odd one), so each SM's tensor core reads half of B from shared
+// memory.  Both CTAs' TMA loads count on the even CTA's full barrier; its
+// commits arrive on both CTAs' stage-free and chunk-ready barriers; both
+// CTAs' eight epilogue warps drain their own 128 rows of TMEM (four chunk
+// accumulators, so the MMAs run up to three chunks ahead of the drain) and
+// arrive on the even CTA's chunk-free barrier.  Every mbarrier wait is bounded; the two
+// CTAs meet in cluster barriers only after setup and before TMEM is freed.
+constexpr int kPairBN = 128, kPairBHalf = kPairBN / 2;
+// warps: 0 producer, 1 MMA (even CTA), 2..9 epilogue (two per TMEM lane quarter, 64 columns each)
+constexpr int kPairEpiWarps = 8, kPairThreads = 32 * (2 + kPairEpiWarps);
+constexpr int kPairAcc = 4;  // chunk accumulators in TMEM (the MMAs run up to three chunks ahead)
+
+template <int STAGES>
+struct PairCfg {
+  static constexpr int P = 2;
+  static constexpr int A_TILE = kTcBM * kTcBK * 2;     // 16 KB
+  static constexpr int B_TILE = kPairBHalf * kTcBK * 2;  // 8 KB
+  static constexpr int STAGE = P * (A_TILE + B_TILE);  // 48 KB
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static constexpr int TMEM_COLS = kPairAcc * kPairBN;  // all 512 columns
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+enum : int { kErrPairProducer = 111, kErrPairMma = 112, kErrPairEpilogue = 113, kErrPairDrain = 114 };
+
+template <int STAGES>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
+    gemm_split_bf16_pair_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
+                                int M, int N, int nk, float alpha, float beta, float* __restrict__ C, int64_t ldc,
+                                int64_t stride_c, int* __restrict__ err) {
+  using Cfg = PairCfg<STAGES>;
+  constexpr int P = Cfg::P;
+  const uint32_t rank = tc::cluster_ctarank();  // 0: issues the MMAs
+  const int bz = blockIdx.z;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* tiles = smem;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * Cfg::STAGE);  // even CTA: both CTAs' bytes
+  uint64_t* empty = full + STAGES;   // both CTAs: the MMAs that read the stage are done
+  uint64_t* tfull = empty + STAGES;      // [kPairAcc] both CTAs: chunk accumulator ready
+  uint64_t* tempty = tfull + kPairAcc;   // [kPairAcc] even CTA: chunk drained by both CTAs' epilogues
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + kPairAcc);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = int(blockIdx.x >> 1) * (2 * kTcBM) + int(rank) * kTcBM;
+  const int n0 = int(blockIdx.y) * kPairBN;
+  const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < kPairAcc; ++b) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], 2 * kPairEpiWarps);  // the epilogue warps of both CTAs
+    }
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc_pair(tmem_slot, Cfg::TMEM_COLS);
+    tc::tmem_relinquish_pair();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();  // the peer's barriers are initialised before anything targets them
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      tc::tma_prefetch_desc(&tma_a);
+      tc::tma_prefetch_desc(&tma_b);
+      const uint32_t full0 = tc::mapa_shared(tc::smem_u32(full), 0);
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
+          atomicExch(err, kErrPairProducer);
+          break;
+        }
+        if (rank == 0) tc::mbar_arrive_expect_tx(&full[s], 2 * Cfg::STAGE);
+        const uint32_t bar = full0 + uint32_t(s) * 8u;
+        uint8_t* st = tiles + s * Cfg::STAGE;
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+          tc::tma_load_3d_pair(st + p * Cfg::A_TILE, &tma_a, bar, kb * kTcBK, m0, bz * P + p);
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+          tc::tma_load_3d_pair(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, bar, kb * kTcBK,
+                               n0 + int(rank) * kPairBHalf, bz * P + p);
+        issued = kb + 1;
+      }
+      // drain (even CTA): every copy of the pair has landed before the CTA exits
+      if (rank == 0)
+        for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
+          if (!tc::mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1)) {
+            atomicExch(err, kErrPairDrain);
+            break;
+          }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && rank == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * kTcBM, kPairBN);
+      bool ok = true;
+      for (int c = 0; c < nchunks && ok; ++c) {
+        const int b = c % kPairAcc;
+        if (!tc::mbar_wait(&tempty[b], ((c / kPairAcc) & 1) ^ 1)) {
+          atomicExch(err, kErrPairMma);
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t acc = tmem + uint32_t(b * kPairBN);
+        const int kb1 = min(nk, (c + 1) * kTcChunk);
+        for (int kb = c * kTcChunk; kb < kb1; ++kb) {
+          const int s = kb % STAGES;
+          if (!tc::mbar_wait(&full[s], (kb / STAGES) & 1)) {
+            atomicExch(err, kErrPairMma);
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint8_t* st = tiles + s * Cfg::STAGE;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            int pa, pb;
+            term_pair(q, pa, pb);
+            const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+            const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+#pragma unroll
+            for (int j = 0; j < kTcBK / 16; ++j)
+              tc::mma_bf16_pair(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+          }
+          tc::mma_commit_pair(&empty[s], 0x3);
+        }
+        if (ok) tc::mma_commit_pair(&tfull[b], 0x3);
+      }
+    }
+  } else {
+    // epilogue warps 2..9: warp w owns TMEM lanes [32*(w%4), +32) (one row of
+    // this CTA's 128 per thread) and columns [64*h, +64), h = (w - 2) / 4
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const int row = q * 32 + lane;
+    const int gm = m0 + row;
+    const uint32_t tempty0 = tc::mapa_shared(tc::smem_u32(tempty), 0);
+    float sum[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) sum[i] = 0.f;
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+      const int b = c % kPairAcc;
+      if (!tc::mbar_wait(&tfull[b], (c / kPairAcc) & 1)) {
+        if (lane == 0) atomicExch(err, kErrPairEpilogue);
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+      uint32_t r0[32], r1[32];
+      const uint32_t base = tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kPairBN + h * 64);
+      tc::tmem_ld_32x32b_x32(base, r0);
+      tc::tmem_ld_32x32b_x32(base + 32u, r1);
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        sum[i] += __uint_as_float(r0[i]);
+        sum[32 + i] += __uint_as_float(r1[i]);
+      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive_cluster(tempty0 + uint32_t(b) * 8u);
+    }
+    if (ok && gm < M) {
+      float* rowp = C + int64_t(bz) * stride_c + int64_t(gm);
+      const int nb = n0 + h * 64;
+#pragma unroll
+      for (int g0 = 0; g0 < 64; g0 += 32) {
+        float cv[32];
+        if (beta != 0.f) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) cv[i] = (nb + g0 + i < N) ? rowp[int64_t(nb + g0 + i) * ldc] : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int gn = nb + g0 + i;
+          if (gn < N) {
+            float v = alpha * sum[g0 + i];
+            if (beta != 0.f) v = fmaf(beta, cv[i], v);
+            rowp[int64_t(gn) * ldc] = v;
+          }
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();  // both CTAs are done with each other's barriers and shared memory
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc_pair(tmem, Cfg::TMEM_COLS);
+  }
+}
+
 // ------------------------------------------------------------ split pass --
 // out[p][r][k] (k < Kp) = term p of X(r, k); X(r, k) = X[r*sr + k*sk]; zero
 // for k >= K.  32x32 tiles through shared memory so both the strided read
@@ -391,8 +601,25 @@ static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const
   return after_launch("gemm_split_bf16");
 }
 
+// 256 x 128 tiles on CTA pairs (x3 only, no split-K): grid x = 2 per 256 rows.
+static gbblas_status_t launch_tc_pair(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb, int64_t M,
+                                      int64_t N, int64_t nk, int64_t batch, float alpha, float beta, float* C,
+                                      int64_t ldc, int64_t stride_c) {
+  constexpr int STAGES = 4;
+  using Cfg = PairCfg<STAGES>;
+  static std::atomic<uint64_t> attr{0};
+  GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(gemm_split_bf16_pair_kernel<STAGES>), Cfg::SMEM,
+                               h->device));
+  dim3 grid(unsigned(2 * cdiv(M, 2 * kTcBM)), unsigned(cdiv(N, kPairBN)), unsigned(batch));
+  if (grid.y > 65535 || grid.z > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
+  gemm_split_bf16_pair_kernel<STAGES><<<grid, kPairThreads, Cfg::SMEM, h->stream>>>(
+      ta, tb, int(M), int(N), int(nk), alpha, beta, C, ldc, stride_c, h->dev_error);
+  return after_launch("gemm_split_bf16_pair");
+}
+
 template <int BN, int P>
-static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& g, int split, int raster_m) {
+static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& g, int split, int raster_m,
+                                      bool pair = false) {
   constexpr int STAGES = (P * (kTcBM + BN) * kTcBK * 2) <= 56 * 1024 ? 4 : ((P * (kTcBM + BN) * kTcBK * 2) <= 72 * 1024 ? 3 : 2);
   const int64_t M = g.m, N = g.n, K = g.k, B = g.batch;
   const int64_t Kp = cdiv(K, kTcBK) * kTcBK;
@@ -416,6 +643,10 @@ static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& 
   GB_TRY(launch_split<P>(h, g.b, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, K, Kp, B, g.stride_b, bt));
   CUtensorMap ma, mb;
   GB_TRY(make_term_map(&ma, at, M, Kp, P * B, kTcBM));
+  if (pair && P == 2 && split == 1) {
+    GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, kPairBHalf));
+    return launch_tc_pair(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
+  }
   GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, BN));
   if (split == 1)
     return launch_tc<BN, P, STAGES, false>(h, ma, mb, M, N, nk, B, 1, g.alpha, g.beta, g.c, g.ldc, g.stride_c,
@@ -439,12 +670,24 @@ gbblas_status_t launch_gemm_split_bf16_cfg(gbblas_handle_t h, const GemmArgs<flo
   return fail(GBBLAS_STATUS_INVALID_ARG, "split-BF16 GEMM: N tile must be 64 or 128");
 }
 
-// The fixed split-BF16 modes: 128 x 128 tiles when they fill the SMs; else
+// CTA-pair tiles for the x3 mode (GBBLAS_PAIR_TILES=0 turns them off).
+static bool pair_tiles_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("GBBLAS_PAIR_TILES");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
+// The fixed split-BF16 modes: 256 x 128 CTA-pair tiles (x3) when there are
+// at least two waves of 128 x 128 tiles; 128 x 128 tiles when they fill the SMs; else
 // 128 x 64 tiles; and when even those leave half the SMs idle, split-K
 // slices of at least 4 k-blocks.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
   const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
+  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled())
+    return split_gemm_run<128, 2>(h, g, 1, 0, true);
   if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 0);
   const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
   int64_t split = 1;
