@@ -246,15 +246,21 @@ extern "C" gbblas_status_t gbblas_grouped_plan_destroy(gbblas_grouped_plan_t pla
 // The persistent kernel hands out tiles longest first (list scheduling), so
 // its makespan is at least the longest tile.  When one problem's tiles are
 // much longer (in K) than the mean work per SM (a few tall-skinny or long-K
-// problems), their K is cut into slices.  A slice costs its k-blocks; the
-// last slice of a tile also folds all S partials, about f k-blocks each
-// (f = 4 for BF16 inputs, 3 for FP32 inputs, whose k-blocks carry six term
-// products), so one tile of nk k-blocks is fastest near S = sqrt(nk / f).
-// Slices stay at least kGtMinSliceK deep, S <= kGtMaxSplits, and the tiles
-// of the whole launch are kept within one wave of sm_count CTAs by halving
-// the largest S first (more tiles than CTAs was measured slower: each extra
-// round re-reads operand panels and the folds queue up).
-constexpr int kGtMaxSplits = 64;
+// problems), their K is cut into slices.  A tile of nk k-blocks cut into S
+// slices costs about nk/S k-blocks for the last slice to finish plus, per
+// level of the fold tree it then climbs, its partial store and ticket (2 f)
+// and the reads of the node's children (f each), f = 2 k-blocks for BF16
+// inputs and 1.5 for FP32 inputs (whose k-blocks carry six term products);
+// the S of least cost is each problem's upper bound.  Slices stay at least
+// kGtMinSliceK deep and S <= kGtMaxSplits.  The launch is then kept within
+// one wave of sm_count CTAs (more tiles than CTAs was measured slower: each
+// extra round re-reads operand panels and the folds queue up) with slices of
+// one common length L: S = ceil(nk / L) under that bound, L the shortest for
+// which the tiles fit, an unsplit tile shorter than L counting as the
+// fraction nk / L of a CTA (short tiles run on the CTAs the slices leave
+// free, one after another).  Equal lengths rather than equal counts keep the
+// longest problem from setting the makespan.
+constexpr int kGtMaxSplits = 256;
 constexpr int64_t kGtMinSliceK = 256;
 
 // K slices of a tile of nk k-blocks under a cap of `cap` k-blocks per slice:
@@ -271,8 +277,15 @@ static void slice_shape(int64_t nk, int64_t cap, int& splits, int& kbs) {
   kbs = int(len);
 }
 
+// Cost in k-blocks of a tile of nk k-blocks in S slices (the rule above).
+static double split_cost(int64_t nk, int64_t S, double f) {
+  double t = double(cdiv(nk, S));
+  for (int64_t n = S; n > 1; n = cdiv(n, kGtFoldFan)) t += f * double(std::min<int64_t>(n, kGtFoldFan) + 2);
+  return t;
+}
+
 // Sets splits / kbs of every problem (k-blocks of `bk` elements; f as above).
-static void plan_splits(std::vector<GroupedProblem>& tab, int bk, int fold_kb, int sm_count) {
+static void plan_splits(std::vector<GroupedProblem>& tab, int bk, double fold_kb, int sm_count) {
   for (GroupedProblem& p : tab) {
     p.splits = 1;
     p.kbs = 0;
@@ -303,25 +316,42 @@ static void plan_splits(std::vector<GroupedProblem>& tab, int bk, int fold_kb, i
   const int64_t min_kb = std::max<int64_t>(1, kGtMinSliceK / bk);
   // nothing to gain unless the longest tile is well above the mean load
   if (nk_max < 2 * min_kb || double(nk_max) <= 2.0 * double(work) / sm_count) return;
-  int64_t tiles = 0;
+  std::vector<int64_t> best(np, 1);  // each problem's S of least cost
   for (size_t i = 0; i < np; ++i) {
-    int64_t s = int64_t(std::sqrt(double(nk[i]) / fold_kb));
-    s = std::min<int64_t>({s, kGtMaxSplits, nk[i] / min_kb});
-    want[i] = std::max<int64_t>(1, s);
-    tiles += out[i] * want[i];
-  }
-  // one wave: halve the largest slice counts until the tiles fit
-  while (tiles > sm_count) {
-    int64_t smax = 1;
-    for (size_t i = 0; i < np; ++i) smax = std::max(smax, want[i]);
-    if (smax == 1) break;
-    for (size_t i = 0; i < np; ++i)
-      if (want[i] == smax) {
-        const int64_t h = std::max<int64_t>(1, smax / 2);
-        tiles -= out[i] * (smax - h);
-        want[i] = h;
+    const int64_t smax = std::min<int64_t>({kGtMaxSplits, int64_t(sm_count), nk[i] / min_kb});
+    double best_cost = split_cost(nk[i], 1, fold_kb);
+    for (int64_t S = 2; S <= smax; ++S) {
+      const double c = split_cost(nk[i], S, fold_kb);
+      if (c < best_cost) {
+        best_cost = c;
+        best[i] = S;
       }
+    }
   }
+  // CTAs the launch occupies with slices of length L (k-blocks)
+  auto slices_at = [&](int64_t L, size_t i) { return std::min<int64_t>(best[i], std::max<int64_t>(1, cdiv(nk[i], L))); };
+  auto load_at = [&](int64_t L) {
+    double t = 0.0;
+    for (size_t i = 0; i < np; ++i) {
+      const int64_t S = slices_at(L, i);
+      t += double(out[i]) * (S > 1 ? double(S) : std::min(1.0, double(nk[i]) / double(L)));
+    }
+    return t;
+  };
+  // the shortest L that fits one wave (load_at does not grow with L)
+  int64_t lo = 1, hi = std::max<int64_t>(1, nk_max);
+  if (load_at(hi) > double(sm_count)) {
+    lo = hi;  // even unsplit the tiles exceed one wave: no split
+  } else {
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (load_at(mid) <= double(sm_count))
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+  }
+  for (size_t i = 0; i < np; ++i) want[i] = slices_at(lo, i);
   for (size_t i = 0; i < np; ++i) {
     if (want[i] > 1) slice_shape(nk[i], cdiv(nk[i], want[i]), tab[i].splits, tab[i].kbs);
     if (tab[i].splits == 1) tab[i].kbs = 0;
@@ -382,7 +412,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
   if (split_bk > 0) {
     // cost model per k-block: a BF16 k-block (one product) is ~3x shorter
     // than an FP32 one (six products), so the fixed costs weigh more
-    plan_splits(tab, split_bk, split_p == 1 ? 4 : 3, sm_count);
+    plan_splits(tab, split_bk, split_p == 1 ? 2.0 : 1.5, sm_count);
   }
   // longest tiles (slices) first; tiles numbered in that order
   auto tile_k = [](const GroupedProblem& p, int bk) { return p.splits > 1 ? int64_t(p.kbs) * bk : int64_t(p.k); };
@@ -401,7 +431,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
       p.part_off = part_floats;
       p.tick_off = n_ticks;
       part_floats += out * p.splits * kGtTileFloats;
-      n_ticks += out * kGtSubs;
+      n_ticks += out * gt_fold_nodes(p.splits) * kGtSubs;
     }
     tiles += nt;
     tile_prob.insert(tile_prob.end(), size_t(nt), int(i));

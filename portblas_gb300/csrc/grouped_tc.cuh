@@ -306,15 +306,34 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
 // Split-K: a problem whose tiles are much longer (in K) than the average work
 // per SM is cut into `splits` K slices per output tile; its tiles are
 // numbered slice-major (tile = slice * output tiles + output tile).  Each
-// epilogue warp owns a 32-row x 64-column sub-block of the output tile; it
-// writes its slice's FP32 partial sub-block (column-major, 32 lanes per
-// column, so the stores coalesce) and takes the sub-block's ticket.  The warp
-// that takes the last ticket adds the slices in index order (deterministic,
-// whatever the arrival order), applies alpha / beta, stores C and resets the
-// ticket, so a graph can replay the launch.  No barrier spans warps.
+// epilogue warp owns a 32-row x 64-column sub-block of the output tile (a
+// sub-block wholly outside the problem is skipped); it writes its slice's
+// FP32 partial sub-block (column-major, 32 lanes per column, so the stores
+// coalesce) and the partials are folded up a tree of fan-in kGtFoldFan:
+// slices 8i .. 8i+7 form node i of level 1, nodes 8j .. 8j+7 of level 1 form
+// node j of level 2, and so on up to one root.  Every node has a ticket per
+// sub-block; the child warp that takes a node's last ticket adds the node's
+// children in index order (so the sum does not depend on the arrival
+// order), resets the ticket (a graph can replay the launch) and, below the
+// root, stores the node's partial in its first child's slot and climbs;
+// the warp that completes the root applies alpha / beta and stores C.  Only
+// the last slice to finish waits for a level's reads, so the fold adds about
+// kGtFoldFan reads per level to the tile instead of one per slice.  No
+// barrier spans warps.
 constexpr int kGtSubs = 8;                  // epilogue sub-blocks per output tile
 constexpr int kGtSubFloats = 32 * 64;       // floats per sub-block
 constexpr int kGtTileFloats = kGtSubs * kGtSubFloats;
+constexpr int kGtFoldFan = 8;
+
+// Internal nodes of the fold tree of `splits` slices (tickets per sub-block).
+__host__ __device__ inline int gt_fold_nodes(int splits) {
+  int t = 0;
+  for (int n = splits; n > 1;) {
+    n = (n + kGtFoldFan - 1) / kGtFoldFan;
+    t += n;
+  }
+  return t;
+}
 
 // One scheduled tile (prob < 0: no more tiles).
 struct GtWork {
@@ -326,7 +345,7 @@ struct GtWork {
   float* c;
   int64_t ldc;
   float* part;           // split-K: slice 0's partial block of this output tile
-  unsigned int* tick;    // split-K: the output tile's kGtSubs tickets
+  unsigned int* tick;    // split-K: the output tile's tickets, [fold node][kGtSubs]
 };
 
 // tiles the scheduler takes from the counter at a time
@@ -425,7 +444,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
             w.kb0 = w.slice * pr.kbs;
             w.nk = min(pr.kbs, nk_all - w.kb0);
             w.part = parts + pr.part_off + int64_t(local) * pr.splits * kGtTileFloats;
-            w.tick = ticks + pr.tick_off + int64_t(local) * kGtSubs;
+            w.tick = ticks + pr.tick_off + int64_t(local) * gt_fold_nodes(pr.splits) * kGtSubs;
           }
           // tiles of a problem go down kGtGroupM M tiles, then along N, so the
           // CTAs working at the same time share A and B panels in L2
@@ -632,25 +651,62 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       }
       if (!ok) break;
       if (w.splits > 1) {
+        // the same sub-blocks are skipped in every slice of the tile
+        if (w.m0 + q * 32 >= w.m || w.n0 + h * 64 >= w.n) continue;
+        // whole 32 x 64 partials, columns and rows beyond the problem
+        // included: unpredicated, the 64 loads of a slice are issued
+        // together (the slots are allocated in full, the extra values unused)
         const int sub = h * 4 + q;
-        float* mine = w.part + (int64_t(w.slice) * kGtSubs + sub) * kGtSubFloats + lane;
+        constexpr int64_t kSlot = int64_t(kGtSubs) * kGtSubFloats;  // floats per slice
+        float* const base = w.part + int64_t(sub) * kGtSubFloats + lane;
+        {
+          float* mine = base + int64_t(w.slice) * kSlot;
 #pragma unroll
-        for (int j = 0; j < 64; ++j) __stcg(mine + j * 32, sum[j]);
-        __threadfence();
-        __syncwarp();
-        unsigned last = 0;
-        if (lane == 0) last = atomicAdd(w.tick + sub, 1u) == unsigned(w.splits - 1) ? 1u : 0u;
-        if (__shfl_sync(0xffffffffu, last, 0) == 0u) continue;
-        __threadfence();
-        const float* src = w.part + int64_t(sub) * kGtSubFloats + lane;
-#pragma unroll
-        for (int j = 0; j < 64; ++j) sum[j] = __ldcg(src + j * 32);
-        for (int sl = 1; sl < w.splits; ++sl) {
-          src += int64_t(kGtSubs) * kGtSubFloats;
-#pragma unroll
-          for (int j = 0; j < 64; ++j) sum[j] += __ldcg(src + j * 32);
+          for (int j = 0; j < 64; ++j) __stcg(mine + j * 32, sum[j]);
         }
-        if (lane == 0) w.tick[sub] = 0u;
+        // climb the fold tree while this warp completes the node above it;
+        // sum holds the value of node idx of the current level
+        int idx = w.slice, nodes = w.splits, node_off = 0;
+        int64_t span = 1;  // slices per node of the current level
+        bool root = false;
+        for (;;) {
+          const int parent = idx / kGtFoldFan, first = parent * kGtFoldFan;
+          const int nchild = min(kGtFoldFan, nodes - first);
+          const int up = (nodes + kGtFoldFan - 1) / kGtFoldFan;
+          unsigned int* t = w.tick + int64_t(node_off + parent) * kGtSubs + sub;
+          __threadfence();
+          __syncwarp();
+          unsigned last = 0;
+          if (lane == 0) last = atomicAdd(t, 1u) == unsigned(nchild - 1) ? 1u : 0u;
+          if (__shfl_sync(0xffffffffu, last, 0) == 0u) break;
+          __threadfence();
+          if (lane == 0) *t = 0u;
+          // a lone child already holds the node's value (and its slot holds it)
+          if (nchild > 1) {
+            const float* src = base + int64_t(first) * span * kSlot;
+#pragma unroll
+            for (int j = 0; j < 64; ++j) sum[j] = __ldcg(src + j * 32);
+            for (int ch = 1; ch < nchild; ++ch) {
+              src += span * kSlot;
+#pragma unroll
+              for (int j = 0; j < 64; ++j) sum[j] += __ldcg(src + j * 32);
+            }
+          }
+          idx = parent;
+          nodes = up;
+          node_off += up;
+          span *= kGtFoldFan;
+          if (nodes == 1) {
+            root = true;
+            break;
+          }
+          if (nchild > 1) {
+            float* dst = base + int64_t(idx) * span * kSlot;
+#pragma unroll
+            for (int j = 0; j < 64; ++j) __stcg(dst + j * 32, sum[j]);
+          }
+        }
+        if (!root) continue;
       }
       const int64_t gm = int64_t(w.m0) + q * 32 + lane;
       if (gm < w.m) {

@@ -180,8 +180,8 @@ def test_grouped_large_problems_tile_grouping(sb, torch_cuda, dtype, method):
 def test_grouped_split_k_long_k(sb, torch_cuda, dtype, method):
     """A few long-K problems beside a small one: the plan cuts their K into
     slices (split-K, tall-skinny); the FP32 partials of the slices are added
-    in slice order by whichever CTA finishes last, so two runs agree bit for
-    bit, and beta is applied once.  Sampled entries against the oracle,
+    up a fixed fold tree (children in index order, whichever CTA arrives
+    last), so two runs agree bit for bit, and beta is applied once.  Sampled entries against the oracle,
     normalised by |alpha| |A||B| + |beta C|."""
     torch = torch_cuda
     from portblas_gb300 import blas
@@ -216,6 +216,55 @@ def test_grouped_split_k_long_k(sb, torch_cuda, dtype, method):
         scale = oracle.gemm_absscale(ta, tb, m, n, k, 1.5, a, lda, b, ldb, 0.5, c, ldc, rows=rows, cols=cols)
         got = p["c"].cpu().numpy().reshape(n, ldc).T[rows, cols]
         assert (np.abs(got - ref) / scale).max() <= 1e-5, (m, n, k)
+    for p, c in zip(probs, c0):
+        p["c"].copy_(c)
+    plan.run()
+    sb.wait()
+    for p, f in zip(probs, first):
+        assert torch.equal(p["c"], f)
+    plan.close()
+    sb.check_device_error()
+
+
+@pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
+@pytest.mark.parametrize("slices", [2, 9, 64, 65, 152])
+def test_grouped_split_k_fold_tree(sb, torch_cuda, method, slices, monkeypatch):
+    """Forced slice counts that give fold trees of one, two and three levels
+    (fan-in 8), with lone children (9, 65) and ragged output tiles (rows not a
+    multiple of 32, N tiles of 2 and 5 columns, whole sub-blocks outside the
+    problem): sampled entries against the oracle, and a second run bit for
+    bit equal to the first (the tickets reset themselves)."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    monkeypatch.setenv("GBBLAS_GROUPED_SPLITK", str(slices))
+    g = rng(300 + slices)
+    # 3 * slices - 1 or 3 * slices k-blocks of 64: every problem gets exactly `slices` slices
+    kb = 3 * slices
+    shapes = [(48, 45, (kb - 1) * 64 - 5, False, False), (200, 130, kb * 64, True, False),
+              (37, 133, (kb - 1) * 64 + 7, False, True)]
+    probs, host = [], []
+    for (m, n, k, ta, tb) in shapes:
+        lda, ldb, ldc = (k if ta else m) + 1, (n if tb else k) + 2, m + 3
+        a = torch.from_numpy(g.uniform(-1, 1, lda * (m if ta else k)).astype(np.float32)).bfloat16()
+        b = torch.from_numpy(g.uniform(-1, 1, ldb * (k if tb else n)).astype(np.float32)).bfloat16()
+        c = g.uniform(-1, 1, ldc * n).astype(np.float32)
+        probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=m, n=n, k=k, alpha=1.5,
+                          a=a.cuda(), lda=lda, b=b.cuda(), ldb=ldb, beta=0.5, c=torch.from_numpy(c).cuda(), ldc=ldc))
+        host.append((ta, tb, m, n, k, a.float().numpy(), lda, b.float().numpy(), ldb, c, ldc))
+    c0 = [p["c"].clone() for p in probs]
+    plan = blas.GroupedPlan(sb, probs, dtype="bfloat16")
+    assert plan.info()[1] == slices
+    plan.run()
+    sb.wait()
+    first = [p["c"].clone() for p in probs]
+    for p, (ta, tb, m, n, k, a, lda, b, ldb, c, ldc) in zip(probs, host):
+        rows = np.concatenate([g.integers(0, m, 40), [m - 1]])
+        cols = np.concatenate([g.integers(0, n, 40), [n - 1]])
+        ref = oracle.gemm(ta, tb, m, n, k, 1.5, a, lda, b, ldb, 0.5, c, ldc, rows=rows, cols=cols)
+        scale = oracle.gemm_absscale(ta, tb, m, n, k, 1.5, a, lda, b, ldb, 0.5, c, ldc, rows=rows, cols=cols)
+        out = p["c"].cpu().numpy().reshape(n, ldc).T
+        assert (np.abs(out[rows, cols] - ref) / scale).max() <= 1e-5, (m, n, k)
+        np.testing.assert_array_equal(out[m:], c.reshape(n, ldc).T[m:])  # padding rows untouched
     for p, c in zip(probs, c0):
         p["c"].copy_(c)
     plan.run()
