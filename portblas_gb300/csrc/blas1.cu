@@ -302,7 +302,8 @@ __device__ __forceinline__ typename Op::Acc block_reduce(typename Op::Acc a, typ
 // loads from the view base (negative increments allowed).
 // Resident CTAs per SM the kernel is compiled for (and the grid is sized
 // to): 4 x 512 threads (32 registers) for FP32, 2 for FP64; nrm2's three
-// accumulators need more than 32 registers, so 3.
+// accumulators, iamax's value-index pairs and dot's two streams need more
+// than 32 registers (at 32, iamax and dot spilled), so 3.
 template <class Op, typename T>
 struct Blas1Occupancy {
   static constexpr int kCtas = sizeof(T) == 4 ? 4 : 2;
@@ -311,6 +312,27 @@ template <>
 struct Blas1Occupancy<Nrm2Op<float>, float> {
   static constexpr int kCtas = 3;
 };
+template <bool IS_MAX>
+struct Blas1Occupancy<IamaxOp<float, IS_MAX>, float> {
+  static constexpr int kCtas = 3;
+};
+template <>
+struct Blas1Occupancy<DotOp<float>, float> {
+  static constexpr int kCtas = 3;
+};
+
+// L2 prefetch of a CTA's first batch: kUnroll runs of blockDim.x 16-byte
+// vectors of x (and y) from vector blockIdx.x * blockDim.x on, nthreads apart.
+__device__ __noinline__ void prefetch_first_batch(const void* x, const void* y, int64_t nv, int64_t nthreads) {
+  for (int u = 0; u < kUnroll; ++u) {
+    const int64_t v = int64_t(blockIdx.x) * blockDim.x + u * nthreads;
+    if (v >= nv) break;
+    const int64_t left = nv - v;
+    const uint32_t bytes = uint32_t(left < int64_t(blockDim.x) ? left : int64_t(blockDim.x)) * 16u;
+    prefetch_l2_bulk(static_cast<const uint8_t*>(x) + v * 16, bytes);
+    if (y) prefetch_l2_bulk(static_cast<const uint8_t*>(y) + v * 16, bytes);
+  }
+}
 
 template <class Op, typename T, bool VEC, bool HAS_Y>
 __global__ void __launch_bounds__(kThreads, Blas1Occupancy<Op, T>::kCtas) blas1_reduce(int64_t n, const T* __restrict__ x, int64_t incx,
@@ -322,10 +344,13 @@ __global__ void __launch_bounds__(kThreads, Blas1Occupancy<Op, T>::kCtas) blas1_
   __shared__ Acc smem[kThreads / 32];
   __shared__ bool is_last;
   pdl_trigger();
-  pdl_wait();  // before any global memory access
-  Acc acc = Op::init();
   const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t nthreads = int64_t(gridDim.x) * blockDim.x;
+  // warm L2 with the CTA's first batch while the previous kernel drains (a
+  // call, so its registers stay out of the main loop's 32)
+  if (VEC && threadIdx.x == 0) prefetch_first_batch(x, HAS_Y ? y : nullptr, n / Vec16<T>::n, nthreads);
+  pdl_wait();  // before any global memory load
+  Acc acc = Op::init();
   if (VEC) {
     using V = Vec16<T>;
     using VT = typename V::type;

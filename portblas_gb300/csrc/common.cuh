@@ -124,6 +124,16 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 
 bool pdl_enabled();
 
+// Brings `bytes` bytes from p into L2 (p 16-byte aligned, bytes a multiple
+// of 16).  A prefetch is only a hint: it changes no value any thread reads
+// (L2 is where every SM's loads and stores meet), so a kernel may warm its
+// first inputs before pdl_wait(), while the previous kernel on the stream is
+// still draining.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(p)), "r"(bytes)
+               : "memory");
+}
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(bool early, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                               cudaStream_t s, Args&&... args) {
