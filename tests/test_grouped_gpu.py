@@ -227,6 +227,50 @@ def test_grouped_split_k_long_k(sb, torch_cuda, dtype, method):
 
 
 @pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
+@pytest.mark.parametrize("shift", [0, 1])
+def test_grouped_bf16_operand_alignment(sb, torch_cuda, method, shift):
+    """BF16 operands moved into the K-major tiles with 32-bit loads: views
+    that start in the odd half of a 4-byte word (shift 1) or on a word
+    (shift 0), each ending exactly at the end of its buffer, odd and even
+    leading dimensions, both transposes, rows and K that are not multiples of
+    the 64 x 64 (transposed) or 8-wide (K-contiguous) pieces: every C entry
+    against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(500 + shift)
+    shapes = [(1, 1, 1), (63, 65, 3), (64, 64, 64), (65, 127, 129), (130, 7, 300), (17, 200, 64), (2, 3, 9),
+              (129, 66, 17)]
+    probs, host, keep = [], [], []
+    for i, (m, n, k) in enumerate(shapes):
+        for ta in (False, True):
+            tb = bool((i + ta) % 2)
+            pa, pb = i % 3, (i + 1) % 2
+            lda, ldb, ldc = (k if ta else m) + pa, (n if tb else k) + pb, m + 1
+            sa, sbs = lda * ((m if ta else k) - 1) + (k if ta else m), ldb * ((k if tb else n) - 1) + (n if tb else k)
+            a = torch.from_numpy(g.uniform(-1, 1, sa).astype(np.float32)).bfloat16()
+            b = torch.from_numpy(g.uniform(-1, 1, sbs).astype(np.float32)).bfloat16()
+            abuf = torch.empty(shift + sa, dtype=torch.bfloat16, device="cuda")
+            bbuf = torch.empty(shift + sbs, dtype=torch.bfloat16, device="cuda")
+            abuf[shift:].copy_(a.cuda())
+            bbuf[shift:].copy_(b.cuda())
+            c = g.uniform(-1, 1, ldc * n).astype(np.float32)
+            keep += [abuf, bbuf]
+            probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=m, n=n, k=k, alpha=1.0,
+                              a=abuf[shift:], lda=lda, b=bbuf[shift:], ldb=ldb, beta=0.5,
+                              c=torch.from_numpy(c).cuda(), ldc=ldc))
+            # the oracle reads lda * cols elements: pad the host copies past the last column
+            ah = np.concatenate([a.float().numpy(), np.zeros(lda, np.float32)])
+            bh = np.concatenate([b.float().numpy(), np.zeros(ldb, np.float32)])
+            host.append((ta, tb, m, n, k, 1.0, ah, lda, bh, ldb, 0.5, c, ldc))
+    plan = blas.GroupedPlan(sb, probs, dtype="bfloat16")
+    plan.run()
+    sb.wait()
+    _check(probs, host)
+    plan.close()
+    sb.check_device_error()
+
+
+@pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
 @pytest.mark.parametrize("slices", [2, 9, 64, 65, 152])
 def test_grouped_split_k_fold_tree(sb, torch_cuda, method, slices, monkeypatch):
     """Forced slice counts that give fold trees of one, two and three levels
