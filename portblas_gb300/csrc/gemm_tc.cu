@@ -285,22 +285,29 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // ---------------------------------------------------- CTA-pair (2-SM) tiles --
-// The 2-term split (x3) on 256 x 128 output tiles, one per cluster of two
-// CTAs: each CTA loads its own 128 rows of A and half (64 rows) of the B
-// tile, so a stage is 48 KB instead of 64 and four fit; the even CTA's MMA
+// The 2-term split (x3) on 256 x 128 output tiles, one at a time per cluster
+// of two CTAs: each CTA loads its own 128 rows of A and half (64 rows) of the
+// B tile, so a stage is 48 KB instead of 64 and four fit; the even CTA's MMA
 // lane issues tcgen05.mma.cta_group::2 (M = 256: A rows 0..127 from the even
 // CTA, 128..255 from the odd one; B columns 0..63 from the even CTA, 64..127
 // from the odd one), so each SM's tensor core reads half of B from shared
 // memory.  Both CTAs' TMA loads count on the even CTA's full barrier; its
 // commits arrive on both CTAs' stage-free and chunk-ready barriers; both
 // CTAs' eight epilogue warps drain their own 128 rows of TMEM (four chunk
-// accumulators, so the MMAs run up to three chunks ahead of the drain) and
-// arrive on the even CTA's chunk-free barrier.  Every mbarrier wait is bounded; the two
-// CTAs meet in cluster barriers only after setup and before TMEM is freed.
+// accumulators) and arrive on the even CTA's chunk-free barrier.
+// Persistent: the grid is the clusters that can be resident at once, and
+// cluster c takes tiles c, c + clusters, ... of a fixed order (batch, then
+// groups of kPairGroupM 256-row tile rows down M, then along N, so the
+// clusters working at the same time share A and B panels in L2).  Stage and
+// chunk counters run on across tiles, so the MMAs of the next tile fill the
+// free accumulators while the epilogue stores C, and the ring never drains
+// at a tile boundary.  Every mbarrier wait is bounded; the two CTAs meet in
+// cluster barriers only after setup and before TMEM is freed.
 constexpr int kPairBN = 128, kPairBHalf = kPairBN / 2;
 // warps: 0 producer, 1 MMA (even CTA), 2..9 epilogue (two per TMEM lane quarter, 64 columns each)
 constexpr int kPairEpiWarps = 8, kPairThreads = 32 * (2 + kPairEpiWarps);
-constexpr int kPairAcc = 4;  // chunk accumulators in TMEM (the MMAs run up to three chunks ahead)
+constexpr int kPairAcc = 4;     // chunk accumulators in TMEM (the MMAs run up to three chunks ahead)
+constexpr int kPairGroupM = 8;  // 256-row tile rows per raster group
 
 template <int STAGES>
 struct PairCfg {
@@ -313,20 +320,33 @@ struct PairCfg {
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
+// Tile t of the fixed order: batch bz, 256-row tile row mp, 128-column tile nt.
+__device__ __forceinline__ void pair_tile(int t, int mp_count, int nt_count, int& bz, int& mp, int& nt) {
+  const int per_batch = mp_count * nt_count;
+  bz = t / per_batch;
+  const int r = t - bz * per_batch;
+  const int per_group = kPairGroupM * nt_count;
+  const int first = (r / per_group) * kPairGroupM, in = r % per_group;
+  const int gsize = min(mp_count - first, kPairGroupM);
+  mp = first + in % gsize;
+  nt = in / gsize;
+}
+
 enum : int { kErrPairProducer = 111, kErrPairMma = 112, kErrPairEpilogue = 113, kErrPairDrain = 114 };
 
 template <int STAGES>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     gemm_split_bf16_pair_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
-                                int M, int N, int nk, float alpha, float beta, float* __restrict__ C, int64_t ldc,
-                                int64_t stride_c, int* __restrict__ err) {
+                                int M, int N, int nk, int tiles, float alpha, float beta, float* __restrict__ C,
+                                int64_t ldc, int64_t stride_c, int* __restrict__ err) {
   using Cfg = PairCfg<STAGES>;
   constexpr int P = Cfg::P;
   const uint32_t rank = tc::cluster_ctarank();  // 0: issues the MMAs
-  const int bz = blockIdx.z;
+  const int cid = int(blockIdx.x >> 1), clusters = int(gridDim.x >> 1);
+  const int mp_count = (M + 2 * kTcBM - 1) / (2 * kTcBM), nt_count = (N + kPairBN - 1) / kPairBN;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* tiles = smem;
+  uint8_t* tiles_smem = smem;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * Cfg::STAGE);  // even CTA: both CTAs' bytes
   uint64_t* empty = full + STAGES;   // both CTAs: the MMAs that read the stage are done
   uint64_t* tfull = empty + STAGES;      // [kPairAcc] both CTAs: chunk accumulator ready
@@ -334,8 +354,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + kPairAcc);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = int(blockIdx.x >> 1) * (2 * kTcBM) + int(rank) * kTcBM;
-  const int n0 = int(blockIdx.y) * kPairBN;
   const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
 
   if (threadIdx.x == 0) {
@@ -364,30 +382,35 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
       tc::tma_prefetch_desc(&tma_a);
       tc::tma_prefetch_desc(&tma_b);
       const uint32_t full0 = tc::mapa_shared(tc::smem_u32(full), 0);
-      int issued = 0;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
-          atomicExch(err, kErrPairProducer);
-          break;
+      uint32_t it = 0;  // k-blocks issued, over all tiles
+      bool ok = true;
+      for (int t = cid; t < tiles && ok; t += clusters) {
+        int bz, mp, nt;
+        pair_tile(t, mp_count, nt_count, bz, mp, nt);
+        const int m0 = mp * (2 * kTcBM) + int(rank) * kTcBM, n0 = nt * kPairBN;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int s = int(it % STAGES);
+          if (!tc::mbar_wait(&empty[s], ((it / STAGES) & 1) ^ 1)) {
+            atomicExch(err, kErrPairProducer);
+            ok = false;
+            break;
+          }
+          if (rank == 0) tc::mbar_arrive_expect_tx(&full[s], 2 * Cfg::STAGE);
+          const uint32_t bar = full0 + uint32_t(s) * 8u;
+          uint8_t* st = tiles_smem + s * Cfg::STAGE;
+#pragma unroll
+          for (int p = 0; p < P; ++p)
+            tc::tma_load_3d_pair(st + p * Cfg::A_TILE, &tma_a, bar, kb * kTcBK, m0, bz * P + p);
+#pragma unroll
+          for (int p = 0; p < P; ++p)
+            tc::tma_load_3d_pair(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, bar, kb * kTcBK,
+                                 n0 + int(rank) * kPairBHalf, bz * P + p);
         }
-        if (rank == 0) tc::mbar_arrive_expect_tx(&full[s], 2 * Cfg::STAGE);
-        const uint32_t bar = full0 + uint32_t(s) * 8u;
-        uint8_t* st = tiles + s * Cfg::STAGE;
-#pragma unroll
-        for (int p = 0; p < P; ++p)
-          tc::tma_load_3d_pair(st + p * Cfg::A_TILE, &tma_a, bar, kb * kTcBK, m0, bz * P + p);
-#pragma unroll
-        for (int p = 0; p < P; ++p)
-          tc::tma_load_3d_pair(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, bar, kb * kTcBK,
-                               n0 + int(rank) * kPairBHalf, bz * P + p);
-        issued = kb + 1;
       }
       // drain (even CTA): every copy of the pair has landed before the CTA exits
       if (rank == 0)
-        for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
-          if (!tc::mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1)) {
+        for (uint32_t j = it > uint32_t(STAGES) ? it - STAGES : 0u; j < it; ++j)
+          if (!tc::mbar_wait(&full[j % STAGES], (j / STAGES) & 1)) {
             atomicExch(err, kErrPairDrain);
             break;
           }
@@ -395,38 +418,42 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
   } else if (warp == 1) {
     if (lane == 0 && rank == 0) {
       constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * kTcBM, kPairBN);
+      uint32_t it = 0, g = 0;  // k-blocks and chunks consumed, over all tiles
       bool ok = true;
-      for (int c = 0; c < nchunks && ok; ++c) {
-        const int b = c % kPairAcc;
-        if (!tc::mbar_wait(&tempty[b], ((c / kPairAcc) & 1) ^ 1)) {
-          atomicExch(err, kErrPairMma);
-          break;
-        }
-        tc::tc_fence_after();
-        const uint32_t acc = tmem + uint32_t(b * kPairBN);
-        const int kb1 = min(nk, (c + 1) * kTcChunk);
-        for (int kb = c * kTcChunk; kb < kb1; ++kb) {
-          const int s = kb % STAGES;
-          if (!tc::mbar_wait(&full[s], (kb / STAGES) & 1)) {
+      for (int t = cid; t < tiles && ok; t += clusters) {
+        for (int c = 0; c < nchunks && ok; ++c, ++g) {
+          const int b = int(g % kPairAcc);
+          if (!tc::mbar_wait(&tempty[b], ((g / kPairAcc) & 1) ^ 1)) {
             atomicExch(err, kErrPairMma);
             ok = false;
             break;
           }
           tc::tc_fence_after();
-          const uint8_t* st = tiles + s * Cfg::STAGE;
+          const uint32_t acc = tmem + uint32_t(b * kPairBN);
+          const int kb1 = min(nk, (c + 1) * kTcChunk);
+          for (int kb = c * kTcChunk; kb < kb1; ++kb, ++it) {
+            const int s = int(it % STAGES);
+            if (!tc::mbar_wait(&full[s], (it / STAGES) & 1)) {
+              atomicExch(err, kErrPairMma);
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint8_t* st = tiles_smem + s * Cfg::STAGE;
 #pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            int pa, pb;
-            term_pair(q, pa, pb);
-            const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
-            const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+            for (int q = 0; q < 3; ++q) {
+              int pa, pb;
+              term_pair(q, pa, pb);
+              const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+              const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
 #pragma unroll
-            for (int j = 0; j < kTcBK / 16; ++j)
-              tc::mma_bf16_pair(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+              for (int j = 0; j < kTcBK / 16; ++j)
+                tc::mma_bf16_pair(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+            }
+            tc::mma_commit_pair(&empty[s], 0x3);
           }
-          tc::mma_commit_pair(&empty[s], 0x3);
+          if (ok) tc::mma_commit_pair(&tfull[b], 0x3);
         }
-        if (ok) tc::mma_commit_pair(&tfull[b], 0x3);
       }
     }
   } else {
@@ -434,51 +461,56 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     // this CTA's 128 per thread) and columns [64*h, +64), h = (w - 2) / 4
     const int q = warp & 3, h = (warp - 2) >> 2;
     const int row = q * 32 + lane;
-    const int gm = m0 + row;
     const uint32_t tempty0 = tc::mapa_shared(tc::smem_u32(tempty), 0);
-    float sum[64];
-#pragma unroll
-    for (int i = 0; i < 64; ++i) sum[i] = 0.f;
+    uint32_t g = 0;  // chunks drained, over all tiles
     bool ok = true;
-    for (int c = 0; c < nchunks; ++c) {
-      const int b = c % kPairAcc;
-      if (!tc::mbar_wait(&tfull[b], (c / kPairAcc) & 1)) {
-        if (lane == 0) atomicExch(err, kErrPairEpilogue);
-        ok = false;
-        break;
-      }
-      tc::tc_fence_after();
-      uint32_t r0[32], r1[32];
-      const uint32_t base = tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kPairBN + h * 64);
-      tc::tmem_ld_32x32b_x32(base, r0);
-      tc::tmem_ld_32x32b_x32(base + 32u, r1);
-      tc::tmem_ld_wait();
+    for (int t = cid; t < tiles && ok; t += clusters) {
+      int bz, mp, nt;
+      pair_tile(t, mp_count, nt_count, bz, mp, nt);
+      const int gm = mp * (2 * kTcBM) + int(rank) * kTcBM + row, n0 = nt * kPairBN;
+      float sum[64];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        sum[i] += __uint_as_float(r0[i]);
-        sum[32 + i] += __uint_as_float(r1[i]);
-      }
-      tc::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive_cluster(tempty0 + uint32_t(b) * 8u);
-    }
-    if (ok && gm < M) {
-      float* rowp = C + int64_t(bz) * stride_c + int64_t(gm);
-      const int nb = n0 + h * 64;
-#pragma unroll
-      for (int g0 = 0; g0 < 64; g0 += 32) {
-        float cv[32];
-        if (beta != 0.f) {
-#pragma unroll
-          for (int i = 0; i < 32; ++i) cv[i] = (nb + g0 + i < N) ? rowp[int64_t(nb + g0 + i) * ldc] : 0.f;
+      for (int i = 0; i < 64; ++i) sum[i] = 0.f;
+      for (int c = 0; c < nchunks; ++c, ++g) {
+        const int b = int(g % kPairAcc);
+        if (!tc::mbar_wait(&tfull[b], (g / kPairAcc) & 1)) {
+          if (lane == 0) atomicExch(err, kErrPairEpilogue);
+          ok = false;
+          break;
         }
+        tc::tc_fence_after();
+        uint32_t r0[32], r1[32];
+        const uint32_t base = tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kPairBN + h * 64);
+        tc::tmem_ld_32x32b_x32(base, r0);
+        tc::tmem_ld_32x32b_x32(base + 32u, r1);
+        tc::tmem_ld_wait();
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
-          const int gn = nb + g0 + i;
-          if (gn < N) {
-            float v = alpha * sum[g0 + i];
-            if (beta != 0.f) v = fmaf(beta, cv[i], v);
-            rowp[int64_t(gn) * ldc] = v;
+          sum[i] += __uint_as_float(r0[i]);
+          sum[32 + i] += __uint_as_float(r1[i]);
+        }
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive_cluster(tempty0 + uint32_t(b) * 8u);
+      }
+      if (ok && gm < M) {
+        float* rowp = C + int64_t(bz) * stride_c + int64_t(gm);
+        const int nb = n0 + h * 64;
+#pragma unroll
+        for (int g0 = 0; g0 < 64; g0 += 32) {
+          float cv[32];
+          if (beta != 0.f) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) cv[i] = (nb + g0 + i < N) ? rowp[int64_t(nb + g0 + i) * ldc] : 0.f;
+          }
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const int gn = nb + g0 + i;
+            if (gn < N) {
+              float v = alpha * sum[g0 + i];
+              if (beta != 0.f) v = fmaf(beta, cv[i], v);
+              rowp[int64_t(gn) * ldc] = v;
+            }
           }
         }
       }
@@ -601,19 +633,42 @@ static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const
   return after_launch("gemm_split_bf16");
 }
 
-// 256 x 128 tiles on CTA pairs (x3 only, no split-K): grid x = 2 per 256 rows.
+// 256 x 128 tiles on CTA pairs (x3 only, no split-K): a persistent grid of
+// the clusters that can be resident at once (two CTAs each).
 static gbblas_status_t launch_tc_pair(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb, int64_t M,
                                       int64_t N, int64_t nk, int64_t batch, float alpha, float beta, float* C,
                                       int64_t ldc, int64_t stride_c) {
   constexpr int STAGES = 4;
   using Cfg = PairCfg<STAGES>;
+  auto* kern = gemm_split_bf16_pair_kernel<STAGES>;
   static std::atomic<uint64_t> attr{0};
-  GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(gemm_split_bf16_pair_kernel<STAGES>), Cfg::SMEM,
-                               h->device));
-  dim3 grid(unsigned(2 * cdiv(M, 2 * kTcBM)), unsigned(cdiv(N, kPairBN)), unsigned(batch));
-  if (grid.y > 65535 || grid.z > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
-  gemm_split_bf16_pair_kernel<STAGES><<<grid, kPairThreads, Cfg::SMEM, h->stream>>>(
-      ta, tb, int(M), int(N), int(nk), alpha, beta, C, ldc, stride_c, h->dev_error);
+  GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(kern), Cfg::SMEM, h->device));
+  const int64_t tiles = cdiv(M, 2 * kTcBM) * cdiv(N, kPairBN) * batch;
+  if (tiles > INT32_MAX / 2) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: too many tiles");
+  // resident clusters, asked once per device (the static schedule assumes
+  // every cluster of the grid runs at the same time)
+  static std::atomic<int> resident[64];
+  int clusters = (h->device >= 0 && h->device < 64) ? resident[h->device].load(std::memory_order_acquire) : 0;
+  if (clusters <= 0) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * unsigned(h->sm_count / 2), 1, 1);
+    cfg.blockDim = dim3(kPairThreads, 1, 1);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = h->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&clusters, reinterpret_cast<const void*>(kern), &cfg));
+    if (clusters < 1) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: no CTA pair can be resident");
+    if (h->device >= 0 && h->device < 64) resident[h->device].store(clusters, std::memory_order_release);
+  }
+  const int64_t grid_clusters = std::min<int64_t>(tiles, clusters);
+  kern<<<dim3(unsigned(2 * grid_clusters)), kPairThreads, Cfg::SMEM, h->stream>>>(
+      ta, tb, int(M), int(N), int(nk), int(tiles), alpha, beta, C, ldc, stride_c, h->dev_error);
   return after_launch("gemm_split_bf16_pair");
 }
 
