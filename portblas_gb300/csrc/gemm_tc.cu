@@ -76,6 +76,7 @@ enum : int { kErrTcProducer = 101, kErrTcMma = 102, kErrTcEpilogue = 103, kErrTc
 // Batches and split-K slices run on gridDim.z (z = batch * split + slice);
 // the operand terms of batch b are terms b*P .. b*P+P-1 of the tensor maps.
 // PARTIAL: split-K slice — the raw tile goes to ws[batch][split][M][N].
+constexpr int kTcGroupM = 16;  // 128-row tile rows per raster group (raster_m == 2)
 template <int BN, int P, int STAGES, bool PARTIAL>
 __global__ void __launch_bounds__(kTcThreads, 1)
     gemm_split_bf16_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b,
@@ -96,9 +97,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // raster_m: consecutive CTAs walk down M (share a B tile) instead of along N
-  const int m0 = (raster_m ? blockIdx.x : blockIdx.y) * kTcBM;
-  const int n0 = (raster_m ? blockIdx.y : blockIdx.x) * BN;
+  // raster_m 1: consecutive CTAs walk down M (share a B tile) instead of
+  // along N; 2: grid (N tiles, M tiles) taken in groups of kTcGroupM tile
+  // rows, down M within a group, so the CTAs resident together share A and
+  // B panels in L2 when neither operand fits there
+  int mt, ntile;
+  if (raster_m == 2) {
+    const int lin = int(blockIdx.y * gridDim.x + blockIdx.x), tn = int(gridDim.x), tm = int(gridDim.y);
+    const int first = (lin / (kTcGroupM * tn)) * kTcGroupM, in = lin % (kTcGroupM * tn);
+    const int gsize = min(tm - first, kTcGroupM);
+    mt = first + in % gsize;
+    ntile = in / gsize;
+  } else {
+    mt = raster_m ? blockIdx.x : blockIdx.y;
+    ntile = raster_m ? blockIdx.y : blockIdx.x;
+  }
+  const int m0 = mt * kTcBM;
+  const int n0 = ntile * BN;
   const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
 
   if (threadIdx.x == 0) {
@@ -623,7 +638,7 @@ static gbblas_status_t launch_tc(gbblas_handle_t h, const CUtensorMap& ta, const
                                Cfg::SMEM, h->device));
   const int kb_per = int(cdiv(nk, split));
   const unsigned tn = unsigned(cdiv(N, BN)), tm = unsigned(cdiv(M, kTcBM));
-  dim3 grid(raster_m ? tm : tn, raster_m ? tn : tm, unsigned(batch * split));
+  dim3 grid(raster_m == 1 ? tm : tn, raster_m == 1 ? tn : tm, unsigned(batch * split));
   if (grid.y > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
   // launched early (PDL): its CTAs set up while the split pass drains
   const cudaError_t le = launch_pdl(true, gemm_split_bf16_kernel<BN, P, STAGES, PARTIAL>, grid, dim3(kTcThreads),
@@ -743,7 +758,7 @@ gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>&
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
   if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled())
     return split_gemm_run<128, 2>(h, g, 1, 0, true);
-  if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 0);
+  if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 2);
   const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
   int64_t split = 1;
   if (2 * t64 <= sm) {
