@@ -29,6 +29,67 @@ struct GemvPolicy {
   }
 };
 
+// ------------------------------------------------- transposed, warp per column --
+// y[j] = alpha * sum_i A[i + j*lda] x[i] + beta * y[j] with one warp per
+// column: lane l reads the 16-byte vectors l, l + 32, ... of the column (and
+// of x, which every warp reads, from L1), kGtwUnroll in flight, then a fixed
+// shuffle tree; no partial sums, no fold, the same order on every run.  The
+// grid is at most one wave (kGtwCtas CTAs of 8 warps per SM, 64 registers,
+// no spills) and column j goes to warp (j / grid) of CTA (j % grid), so the
+// CTAs get the same number of columns to within one.  Taken for x
+// contiguous, 16-byte-aligned columns and x, and between a quarter and two
+// columns per warp of the wave; outside that range the TMA column sweep
+// (fewer columns leave too few loads in flight, more leave a ragged last
+// round: 16384^2 measured 160 us here against 154 for the sweep).  Not
+// launched early: placed early, its CTAs shared SMs with the GEMV before it
+// and the nine-op step ran 51 us longer, though each op alone was faster.
+constexpr int kGtwUnroll = 4, kGtwCtas = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(kMvThreads, kGtwCtas)
+    gemv_t_warp_cols(GemvPolicy<T> pol, int64_t m, int64_t n, const T* __restrict__ A, int64_t lda,
+                     const T* __restrict__ x) {
+  using V = typename Pack16<T>::V;
+  constexpr int W = Pack16<T>::n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nv = m / W;  // whole vectors per column
+  const int64_t step = int64_t(kMvWarps) * gridDim.x;
+  const int64_t first = int64_t(warp) * gridDim.x + blockIdx.x;
+  const V* xv = reinterpret_cast<const V*>(x);
+  for (int64_t j = first; j < n; j += step) {
+    const V* av = reinterpret_cast<const V*>(A + j * lda);
+    T acc = T(0);
+    int64_t v = lane;
+    for (; v + 32 * (kGtwUnroll - 1) < nv; v += 32 * kGtwUnroll) {
+      V a[kGtwUnroll], b[kGtwUnroll];
+#pragma unroll
+      for (int u = 0; u < kGtwUnroll; ++u) {
+        a[u] = __ldcs(av + v + 32 * u);
+        b[u] = __ldg(xv + v + 32 * u);
+      }
+#pragma unroll
+      for (int u = 0; u < kGtwUnroll; ++u) {
+        T ae[W], be[W];
+        Pack16<T>::get(a[u], ae);
+        Pack16<T>::get(b[u], be);
+#pragma unroll
+        for (int e = 0; e < W; ++e) acc = fma(ae[e], be[e], acc);
+      }
+    }
+    for (; v < nv; v += 32) {
+      T ae[W], be[W];
+      Pack16<T>::get(__ldcs(av + v), ae);
+      Pack16<T>::get(__ldg(xv + v), be);
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc = fma(ae[e], be[e], acc);
+    }
+    for (int64_t i = nv * W + lane; i < m; i += 32) acc = fma(A[j * lda + i], x[i], acc);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) pol.finish(acc, j);
+  }
+}
+
 template <typename T>
 gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T alpha, const T* a, int64_t lda,
                           const T* x, int64_t incx, T beta, T* y, int64_t incy) {
@@ -64,6 +125,14 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
     return after_launch("gemv_n");
   }
   {
+    // one column per warp where that fits in one wave, else the full wave
+    const int64_t slots = int64_t(kGtwCtas) * h->sm_count, warps = slots * kMvWarps;
+    const int64_t want = cdiv(n, int64_t(kMvWarps));
+    const int64_t grid = want < slots ? want : slots;
+    if (incx == 1 && vec && aligned16(x) && m > 0 && 4 * n >= warps && n <= 2 * warps) {
+      gemv_t_warp_cols<T><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, m, n, a, lda, x);
+      return after_launch("gemv_t_warp_cols");
+    }
     gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
     if (try_cols_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;
   }

@@ -103,3 +103,30 @@ def test_gemv_tma_stream_path(sb, torch_cuda, trans, m, n, lda, beta):
     mask = np.ones(len(y), bool)
     mask[: ylen * 3: 3] = False
     np.testing.assert_array_equal(yo[mask], y[mask])
+
+
+@pytest.mark.parametrize("m,n,lda", [(1001, 2500, 1004), (3, 3000, 4), (4096, 9728, 4096), (130, 1300, 132)])
+@pytest.mark.parametrize("beta,incy", [(0.0, 1), (0.5, 3)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_gemv_t_warp_per_column_path(sb, torch_cuda, m, n, lda, beta, incy, dtype):
+    """Transposed GEMV over many columns with contiguous x and 16-byte-aligned
+    columns (one warp per column): ragged column lengths (vector part plus
+    scalar tail, or the tail alone), up to two columns per warp, strided y;
+    every entry against the oracle and y's gaps untouched."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(m + n + lda + incy)
+    a = g.uniform(-1, 1, lda * n).astype(dtype)
+    x = g.uniform(-1, 1, m).astype(dtype)
+    y = g.uniform(-1, 1, n * incy).astype(dtype)
+    ref = oracle.gemv("t", m, n, 1.25, a, lda, x, 1, beta, y, incy)
+    yd = to_dev(y, torch)
+    blas._gemv(sb, "t", m, n, 1.25, to_dev(a, torch), lda, to_dev(x, torch), 1, beta, yd, incy)
+    got = oracle.view(to_host(yd), n, incy)
+    tol = 2e-5 if dtype == np.float32 else 1e-12
+    np.testing.assert_allclose(got, ref, rtol=tol, atol=tol * np.abs(ref).max())
+    if incy > 1:
+        yo = to_host(yd)
+        mask = np.ones(len(y), bool)
+        mask[::incy] = False
+        np.testing.assert_array_equal(yo[mask], y[mask])
