@@ -30,8 +30,9 @@
 //                 N128 for every term pair of one or two terms, and for three
 //                 terms the six products as four MMAs, two of them N256 over
 //                 adjacent B terms), commits each stage back to the producer
-//                 and each finished chunk of CHUNK k-blocks to one of two
-//                 TMEM accumulators;
+//                 and each finished chunk of CHUNK k-blocks to one of the
+//                 TMEM accumulators (four of 128 columns for BF16 inputs, two
+//                 of 256 for FP32);
 //      warps 3-10 epilogue: tcgen05.ld of each chunk into FP32 registers
 //                 (64 columns of one output row per thread), then
 //                 alpha / beta and the stores to C (or, for a K slice, the
@@ -54,8 +55,6 @@ constexpr int kGtBM = 128, kGtBN = 128, kGtBK = 64, kGtEpiWarps = 8, kGtThreads 
 // K depth of one TMEM chunk before its promotion into FP32 registers (a
 // shallower chunk keeps more of the sum in FP32; 128 costs no time here)
 constexpr int kGtChunkK = 128;
-// TMEM chunk accumulators (the MMA warp runs up to kGtAcc - 1 chunks ahead of the epilogue)
-constexpr int kGtAcc = 2;
 
 template <int P>
 struct GtCfg {
@@ -66,15 +65,19 @@ struct GtCfg {
   static constexpr int B_TILE = kGtBN * BK * 2;
   static constexpr int STAGE = P * (A_TILE + B_TILE);
   static constexpr int STAGES = P == 1 ? 6 : (P == 2 ? 3 : 4);
+  // TMEM chunk accumulators (the MMA warp runs up to NACC - 1 chunks ahead
+  // of the epilogue): four of 128 columns for one or two terms, two of 256
+  // for three
+  static constexpr int NACC = P == 3 ? 2 : 4;
   // barriers: full/empty per stage, two accumulator pairs, a work-slot pair per ring entry; then the TMEM address
-  static constexpr int BARRIER_BYTES = (2 * STAGES + 2 * kGtAcc + 2 * kGtRing) * 8 + 4;
+  static constexpr int BARRIER_BYTES = (2 * STAGES + 2 * NACC + 2 * kGtRing) * 8 + 4;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
   static constexpr int NPAIRS = P == 1 ? 1 : 3;  // term products issued one by one (P <= 2)
   // columns of one chunk accumulator: with P = 3 the products of an A term
   // with the two adjacent leading B terms are one N = 256 MMA, and the
   // epilogue adds the two column halves
   static constexpr int ACC = P == 3 ? 2 * kGtBN : kGtBN;
-  static constexpr int TMEM_COLS = kGtAcc * ACC;  // the chunk accumulators
+  static constexpr int TMEM_COLS = NACC * ACC;  // the chunk accumulators
   static_assert(TMEM_COLS <= 512, "tensor memory budget");
   static_assert(BARRIER_BYTES <= 512, "barrier area");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
@@ -377,9 +380,10 @@ __global__ void __launch_bounds__(kGtThreads, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * Cfg::STAGE);
   uint64_t* empty = full + S;
-  uint64_t* tfull = empty + S;         // [kGtAcc] chunk accumulator ready
-  uint64_t* tempty = tfull + kGtAcc;   // [kGtAcc] chunk accumulator drained
-  uint64_t* wfull = tempty + kGtAcc;   // [kGtRing] work slot published
+  constexpr int NACC = Cfg::NACC;
+  uint64_t* tfull = empty + S;         // [NACC] chunk accumulator ready
+  uint64_t* tempty = tfull + NACC;     // [NACC] chunk accumulator drained
+  uint64_t* wfull = tempty + NACC;     // [kGtRing] work slot published
   uint64_t* wempty = wfull + kGtRing;  // [kGtRing] work slot read by the producer, MMA warp and epilogue
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wempty + kGtRing);
   __shared__ GtWork ring[kGtRing];
@@ -390,7 +394,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < kGtAcc; ++b) {
+    for (int b = 0; b < NACC; ++b) {
       tc::mbar_init(&tfull[b], 1);
       tc::mbar_init(&tempty[b], kGtEpiWarps);  // one arrival per epilogue warp
     }
@@ -549,8 +553,8 @@ __global__ void __launch_bounds__(kGtThreads, 1)
         if (w.prob < 0) break;
         const int nch = (w.nk + CHUNK - 1) / CHUNK;
         for (int c = 0; c < nch && ok; ++c, ++g) {
-          const int b = g % kGtAcc;
-          if (!tc::mbar_wait(&tempty[b], ((g / kGtAcc) & 1) ^ 1)) {
+          const int b = g % NACC;
+          if (!tc::mbar_wait(&tempty[b], ((g / NACC) & 1) ^ 1)) {
             atomicExch(err, kErrGtMma);
             ok = false;
             break;
@@ -627,8 +631,8 @@ __global__ void __launch_bounds__(kGtThreads, 1)
       const int nch = (w.nk + CHUNK - 1) / CHUNK;
       bool ok = true;
       for (int c = 0; c < nch; ++c, ++g) {
-        const int b = g % kGtAcc;
-        if (!tc::mbar_wait(&tfull[b], (g / kGtAcc) & 1)) {
+        const int b = g % NACC;
+        if (!tc::mbar_wait(&tfull[b], (g / NACC) & 1)) {
           if (lane == 0) atomicExch(err, kErrGtEpilogue);
           ok = false;
           break;
