@@ -542,44 +542,70 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
 
 // ------------------------------------------------------------ split pass --
 // out[p][r][k] (k < Kp) = term p of X(r, k); X(r, k) = X[r*sr + k*sk]; zero
-// for k >= K.  32x32 tiles through shared memory so both the strided read
-// and the K-contiguous write are coalesced.
+// for k >= K; Kp is a multiple of 64.  One CTA per 64 x 64 tile, 256
+// threads; thread t writes the eight k from 8 (t % 8) of rows t / 8 and
+// t / 8 + 32 of the tile, one 16-byte store per row and term.  K-contiguous
+// operands (sk == 1) are read straight into registers (two 16-byte loads per
+// row when rows are 16-byte aligned); others are transposed through shared
+// memory, each thread with 16 loads in flight along the contiguous rows.
 template <int P>
 __global__ void __launch_bounds__(256) split_bf16_kernel(const float* __restrict__ X, int64_t sr, int64_t sk,
                                                          int64_t R, int64_t K, int64_t Kp, int64_t xstride,
-                                                         __nv_bfloat16* __restrict__ out) {
+                                                         int vec4, __nv_bfloat16* __restrict__ out) {
   pdl_trigger();  // the GEMM that reads the terms may place its CTAs and set up meanwhile
-  __shared__ float t[32][33];  // t[k][r]
+  __shared__ float t[64][65];  // t[k][r]
   X += int64_t(blockIdx.z) * xstride;
   out += int64_t(blockIdx.z) * P * R * Kp;
-  const int64_t r0 = int64_t(blockIdx.y) * 32, k0 = int64_t(blockIdx.x) * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  if (sr == 1) {
+  const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
+  const int tid = threadIdx.x, c = tid & 7;
+  const int64_t k = k0 + 8 * c;
+  float x[2][8];
+  if (sk == 1) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int64_t k = k0 + ty + 8 * i, r = r0 + tx;
-      t[ty + 8 * i][tx] = (r < R && k < K) ? X[r + k * sk] : 0.f;
+    for (int h = 0; h < 2; ++h) {
+      const int64_t r = r0 + (tid >> 3) + 32 * h;
+      const float* q = X + r * sr + k;
+      if (r < R && vec4 && k + 8 <= K) {
+        const float4 a = __ldcs(reinterpret_cast<const float4*>(q));
+        const float4 b = __ldcs(reinterpret_cast<const float4*>(q + 4));
+        x[h][0] = a.x; x[h][1] = a.y; x[h][2] = a.z; x[h][3] = a.w;
+        x[h][4] = b.x; x[h][5] = b.y; x[h][6] = b.z; x[h][7] = b.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[h][e] = (r < R && k + e < K) ? __ldcs(q + e) : 0.f;
+      }
     }
   } else {
+    const int rr = tid & 63, kq = tid >> 6;
+    const bool rok = r0 + rr < R;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int64_t r = r0 + ty + 8 * i, k = k0 + tx;
-      t[tx][ty + 8 * i] = (r < R && k < K) ? X[r * sr + k * sk] : 0.f;
+    for (int i = 0; i < 16; ++i) {
+      const int64_t kk = k0 + kq + 4 * i;
+      t[kq + 4 * i][rr] = (rok && kk < K) ? __ldcs(X + (r0 + rr) * sr + kk * sk) : 0.f;
     }
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[h][e] = t[8 * c + e][(tid >> 3) + 32 * h];
   }
-  __syncthreads();
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int64_t r = r0 + ty + 8 * i, k = k0 + tx;
-    if (r < R && k < Kp) {
-      float x = t[tx][ty + 8 * i];
-      const int64_t o = r * Kp + k;
+  for (int h = 0; h < 2; ++h) {
+    const int64_t r = r0 + (tid >> 3) + 32 * h;
+    if (r >= R) continue;
+    __nv_bfloat16* o = out + r * Kp + k;
 #pragma unroll
-      for (int p = 0; p < P; ++p) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(x);
-        out[int64_t(p) * R * Kp + o] = h;
-        x = x - __bfloat162float(h);  // exact residual
+    for (int p = 0; p < P; ++p) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(x[h][2 * e], x[h][2 * e + 1]);
+        w[e] = *reinterpret_cast<const uint32_t*>(&h2);
+        x[h][2 * e] -= __uint_as_float(w[e] << 16);  // exact residuals
+        x[h][2 * e + 1] -= __uint_as_float(w[e] & 0xffff0000u);
       }
+      // plain stores: a small GEMM finds its terms still in L2
+      *reinterpret_cast<uint4*>(o + int64_t(p) * R * Kp) = make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
 }
@@ -622,9 +648,10 @@ static gbblas_status_t make_term_map(CUtensorMap* map, void* base, int64_t rows,
 template <int P>
 static gbblas_status_t launch_split(gbblas_handle_t h, const float* X, int64_t sr, int64_t sk, int64_t R, int64_t K,
                                     int64_t Kp, int64_t batch, int64_t xstride, __nv_bfloat16* out) {
-  dim3 grid(unsigned(Kp / 32), unsigned(cdiv(R, 32)), unsigned(batch));
+  dim3 grid(unsigned(Kp / 64), unsigned(cdiv(R, 64)), unsigned(batch));
   if (grid.y > 65535 || grid.z > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
-  split_bf16_kernel<P><<<grid, dim3(32, 8), 0, h->stream>>>(X, sr, sk, R, K, Kp, xstride, out);
+  const int vec4 = sk == 1 && sr % 4 == 0 && xstride % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  split_bf16_kernel<P><<<grid, 256, 0, h->stream>>>(X, sr, sk, R, K, Kp, xstride, vec4, out);
   return after_launch("split_bf16");
 }
 
