@@ -548,15 +548,27 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
 // operands (sk == 1) are read straight into registers (two 16-byte loads per
 // row when rows are 16-byte aligned); others are transposed through shared
 // memory, each thread with 16 loads in flight along the contiguous rows.
+// One operand of the split pass (A or B of the GEMM).
+struct SplitOperand {
+  const float* X;
+  int64_t sr, sk, R, xstride;
+  int vec4;  // sk == 1 with 16-byte-aligned rows
+  __nv_bfloat16* out;
+};
+
+// Both operands in one launch: blockIdx.z = 2 * batch + operand; tiles past
+// an operand's rows exit at once.
 template <int P>
-__global__ void __launch_bounds__(256) split_bf16_kernel(const float* __restrict__ X, int64_t sr, int64_t sk,
-                                                         int64_t R, int64_t K, int64_t Kp, int64_t xstride,
-                                                         int vec4, __nv_bfloat16* __restrict__ out) {
+__global__ void __launch_bounds__(256) split_bf16_kernel(SplitOperand a, SplitOperand b, int64_t K, int64_t Kp) {
   pdl_trigger();  // the GEMM that reads the terms may place its CTAs and set up meanwhile
   __shared__ float t[64][65];  // t[k][r]
-  X += int64_t(blockIdx.z) * xstride;
-  out += int64_t(blockIdx.z) * P * R * Kp;
+  const SplitOperand& op = (blockIdx.z & 1) ? b : a;
+  const int64_t R = op.R, sr = op.sr, sk = op.sk;
+  const int vec4 = op.vec4;
   const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
+  if (r0 >= R) return;
+  const float* __restrict__ X = op.X + int64_t(blockIdx.z >> 1) * op.xstride;
+  __nv_bfloat16* __restrict__ out = op.out + int64_t(blockIdx.z >> 1) * P * R * Kp;
   const int tid = threadIdx.x, c = tid & 7;
   const int64_t k = k0 + 8 * c;
   float x[2][8];
@@ -645,14 +657,31 @@ static gbblas_status_t make_term_map(CUtensorMap* map, void* base, int64_t rows,
   return GBBLAS_STATUS_SUCCESS;
 }
 
-template <int P>
-static gbblas_status_t launch_split(gbblas_handle_t h, const float* X, int64_t sr, int64_t sk, int64_t R, int64_t K,
-                                    int64_t Kp, int64_t batch, int64_t xstride, __nv_bfloat16* out) {
-  dim3 grid(unsigned(Kp / 64), unsigned(cdiv(R, 64)), unsigned(batch));
-  if (grid.y > 65535 || grid.z > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
+static SplitOperand split_operand(const float* X, int64_t sr, int64_t sk, int64_t R, int64_t xstride,
+                                  __nv_bfloat16* out) {
   const int vec4 = sk == 1 && sr % 4 == 0 && xstride % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
-  split_bf16_kernel<P><<<grid, 256, 0, h->stream>>>(X, sr, sk, R, K, Kp, xstride, vec4, out);
-  return after_launch("split_bf16");
+  return SplitOperand{X, sr, sk, R, xstride, vec4, out};
+}
+
+// The terms of A and B, one launch.
+template <int P>
+static gbblas_status_t launch_split(gbblas_handle_t h, const SplitOperand& a, const SplitOperand& b, int64_t K,
+                                    int64_t Kp, int64_t batch) {
+  const int64_t rt = cdiv(a.R > b.R ? a.R : b.R, 64);
+  if (rt > 65535) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: grid too large");
+  constexpr int64_t kMaxBatch = 65535 / 2;  // grid z = 2 per batch entry
+  for (int64_t b0 = 0; b0 < batch; b0 += kMaxBatch) {
+    const int64_t nb = batch - b0 < kMaxBatch ? batch - b0 : kMaxBatch;
+    SplitOperand ac = a, bc = b;
+    ac.X = a.X + b0 * a.xstride;
+    bc.X = b.X + b0 * b.xstride;
+    ac.out = a.out + b0 * P * a.R * Kp;
+    bc.out = b.out + b0 * P * b.R * Kp;
+    dim3 grid(unsigned(Kp / 64), unsigned(rt), unsigned(2 * nb));
+    split_bf16_kernel<P><<<grid, 256, 0, h->stream>>>(ac, bc, K, Kp);
+    GB_TRY(after_launch("split_bf16"));
+  }
+  return GBBLAS_STATUS_SUCCESS;
 }
 
 template <int BN, int P, int STAGES, bool PARTIAL>
@@ -736,8 +765,8 @@ static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& 
   auto* bt = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(wsp) + a_bytes);
   float* ws = split > 1 ? reinterpret_cast<float*>(static_cast<uint8_t*>(wsp) + a_bytes + b_bytes) : nullptr;
   // A(m, k): (ta ? A[k + m*lda] : A[m + k*lda]);  B as rows n: (tb ? B[n + k*ldb] : B[k + n*ldb])
-  GB_TRY(launch_split<P>(h, g.a, g.ta ? g.lda : 1, g.ta ? 1 : g.lda, M, K, Kp, B, g.stride_a, at));
-  GB_TRY(launch_split<P>(h, g.b, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, K, Kp, B, g.stride_b, bt));
+  GB_TRY(launch_split<P>(h, split_operand(g.a, g.ta ? g.lda : 1, g.ta ? 1 : g.lda, M, g.stride_a, at),
+                         split_operand(g.b, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, g.stride_b, bt), K, Kp, B));
   CUtensorMap ma, mb;
   GB_TRY(make_term_map(&ma, at, M, Kp, P * B, kTcBM));
   if (pair && P == 2 && split == 1) {
