@@ -391,6 +391,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
   tc::cluster_sync();  // the peer's barriers are initialised before anything targets them
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  pdl_wait();  // the operand terms (and C) are written by earlier kernels on the stream
 
   if (warp == 0) {
     if (lane == 0) {
@@ -738,8 +739,12 @@ static gbblas_status_t launch_tc_pair(gbblas_handle_t h, const CUtensorMap& ta, 
     if (h->device >= 0 && h->device < 64) resident[h->device].store(clusters, std::memory_order_release);
   }
   const int64_t grid_clusters = std::min<int64_t>(tiles, clusters);
-  kern<<<dim3(unsigned(2 * grid_clusters)), kPairThreads, Cfg::SMEM, h->stream>>>(
-      ta, tb, int(M), int(N), int(nk), int(tiles), alpha, beta, C, ldc, stride_c, h->dev_error);
+  // placed early (programmatic dependent launch) while the split pass
+  // drains; the grid is the resident clusters, so it cannot land unevenly
+  const cudaError_t le = launch_pdl(true, kern, dim3(unsigned(2 * grid_clusters)), dim3(kPairThreads), Cfg::SMEM,
+                                    h->stream, ta, tb, int(M), int(N), int(nk), int(tiles), alpha, beta, C, ldc,
+                                    stride_c, h->dev_error);
+  if (le != cudaSuccess) return cuda_fail(le, "gemm_split_bf16_pair");
   return after_launch("gemm_split_bf16_pair");
 }
 
