@@ -260,7 +260,8 @@ gbblas_status_t gbblas_dsymm(gbblas_handle_t h, char side, char uplo, int64_t m,
  * src/interface/blas3/backend/nvidia_gpu.hpp:116-171).  FP32: configs 0..19
  * are SIMT tiles {128x128, 128x64, 64x128, 64x64} x split-K {1,2,4,8,16},
  * 20..39 the 3-term split-BF16 tcgen05 kernel with N tile {128, 64} x
- * split-K {1,2,4,8,16} x raster {N, M}; all are FP32-accurate.  FP64:
+ * split-K {1,2,4,8,16} x raster (raster_m 2: groups of 16 tile rows down M,
+ * then along N; 1: down M); all are FP32-accurate.  FP64:
  * configs 40..59 are SIMT tiles x split-K as 0..19.  AUTO picks one of the
  * element type's configs per call (autotuned winner > learned selector >
  * size heuristic).  config_info takes any config (method 0 FP32 SIMT,

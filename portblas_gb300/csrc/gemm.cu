@@ -61,9 +61,16 @@ gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g) {
     case GBBLAS_SGEMM_SPLIT_BF16X6: return launch_gemm_split_bf16(h, g, 3);
     default: break;
   }
-  // AUTO: many small problems go to the one-CTA-per-problem kernel; otherwise
-  // every config is FP32-accurate and the selector picks one
+  // AUTO: many small problems go to the one-CTA-per-problem kernel; shapes
+  // beyond the largest the selector was trained on (2 m n k batch > 2^35
+  // flop) that were not autotuned take the fixed x6 path (FP32-accurate,
+  // grouped-raster 128 x 128 tiles: 8192^3 at 274 TFLOP/s against 236 for
+  // the selector's extrapolated pick); otherwise every config is
+  // FP32-accurate and the selector picks one
   if (small_batched_applies(g, h->sm_count)) return launch_gemm_small_batched(h, g);
+  if (2.0 * double(g.m) * double(g.n) * double(g.k) * double(g.batch) > double(int64_t(1) << 35) &&
+      !has_tuned_config(g))
+    return launch_gemm_split_bf16(h, g, 3);
   gbblas_status_t s = launch_sgemm_config(h, g, select_sgemm_config(h, g));
   if (s != GBBLAS_STATUS_UNSUPPORTED) return s;
   clear_error();  // a config that cannot take this shape (grid / workspace limits)

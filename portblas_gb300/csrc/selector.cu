@@ -8,7 +8,8 @@
 //   configs  0..19  FP32 SIMT, CTA tile {128x128, 128x64, 64x128, 64x64} x
 //                   split-K {1, 2, 4, 8, 16}
 //   configs 20..39  FP32 as 3-term split-BF16 on tcgen05, N tile {128, 64} x
-//                   split-K {1, 2, 4, 8, 16} x raster {along N, along M}
+//                   split-K {1, 2, 4, 8, 16} x raster {grouped (16 tile rows
+//                   down M, then along N), down M}
 //   configs 40..59  FP64 SIMT, CTA tile {128x128, 128x64, 64x128, 64x64} x
 //                   split-K {1, 2, 4, 8, 16}
 // All FP32 configs are FP32-accurate, so AUTO may pick any of them.  The
@@ -61,7 +62,7 @@ static SgemmConfig config_of(int c) {
   s.tile_m = 128;
   s.tile_n = i < 10 ? 128 : 64;
   s.split = kSplits[(i % 10) / 2];
-  s.raster_m = i % 2;
+  s.raster_m = i % 2 ? 1 : 2;  // raster codes of launch_gemm_split_bf16_cfg
   return s;
 }
 
@@ -238,6 +239,11 @@ static int select_config(const GemmArgs<T>& g) {
 }
 
 int select_sgemm_config(gbblas_handle_t, const GemmArgs<float>& g) { return select_config(g); }
+
+bool has_tuned_config(const GemmArgs<float>& g) {
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  return tuned().count(shape_key(g)) != 0;
+}
 int select_dgemm_config(gbblas_handle_t, const GemmArgs<double>& g) { return select_config(g); }
 
 static gbblas_status_t launch_config(gbblas_handle_t h, const GemmArgs<float>& g, int c) {

@@ -22,6 +22,7 @@ gbblas_status_t launch_dgemm_config(gbblas_handle_t h, const GemmArgs<double>& g
 // the learned selector when its weights are loaded, else the fixed
 // size-threshold heuristic; always one of the element type's configs.
 int select_sgemm_config(gbblas_handle_t h, const GemmArgs<float>& g);
+bool has_tuned_config(const GemmArgs<float>& g);  // an autotuned winner is stored for this shape
 int select_dgemm_config(gbblas_handle_t h, const GemmArgs<double>& g);
 
 // The fixed size-threshold heuristic alone.
