@@ -22,9 +22,13 @@
 //               a0 b2 and a2 b0 into the second column half), both steps of a
 //               pair into one of two accumulators, so the next pair runs
 //               while the epilogue drains this one;
-//   warps 10-13 epilogue: each thread one row of one problem (TMEM lane
-//               r < 64: problem p, columns 0..63; else q, columns 64..127),
-//               both column halves summed, alpha / beta, stores to C.
+//   warps 10-17 epilogue: two warps per TMEM lane quarter, each thread one
+//               row of one problem (TMEM lane r < 64: problem p, columns
+//               0..63; else q, columns 64..127) and 32 of its 64 columns,
+//               both column halves summed, alpha / beta, stores to C.  (With
+//               four warps the epilogue was busy 77% of the kernel and held
+//               the accumulators, the term stages and the raw ring behind
+//               it; per-role clock counters.)
 // Every mbarrier wait is bounded; a wait that gives up records an error
 // code, the producer waits for its copies in flight and TMEM is freed.
 #include <cuda_bf16.h>
@@ -40,8 +44,8 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 EncodeTiledFn tensor_map_encoder();  // gemm_tc.cu
 
-constexpr int kBtThreads = 14 * 32;
-constexpr int kBtConvWarps = 8, kBtFirstConv = 2, kBtFirstEpi = kBtFirstConv + kBtConvWarps;
+constexpr int kBtConvWarps = 8, kBtEpiWarps = 8, kBtFirstConv = 2, kBtFirstEpi = kBtFirstConv + kBtConvWarps;
+constexpr int kBtThreads = (kBtFirstEpi + kBtEpiWarps) * 32;
 constexpr int kBtRawSlot = 64 * 32 * 4;        // one operand's raw FP32 k-half (8 KB)
 constexpr int kBtRawStage = 4 * kBtRawSlot;    // A_p, A_q, B_p, B_q
 constexpr int kBtRawStages = 4;
@@ -114,7 +118,7 @@ __global__ void __launch_bounds__(kBtThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&afull[b], 1);
-      tc::mbar_init(&aempty[b], 4);  // one arrival per epilogue warp
+      tc::mbar_init(&aempty[b], kBtEpiWarps);  // one arrival per epilogue warp
     }
     tc::fence_mbar_init();
   }
@@ -267,6 +271,7 @@ __global__ void __launch_bounds__(kBtThreads, 1)
   } else {
     // ------------------------------------------------------------ epilogue --
     const int q = warp & 3;  // TMEM lanes 32q .. 32q+31
+    const int c0 = 32 * ((warp - kBtFirstEpi) >> 2);  // this warp's 32 of the 64 columns
     const int R = 32 * q + lane;
     const int i = R & 63, half = R >> 6;  // row of problem 2*pair + half
     uint32_t it = 0;
@@ -277,35 +282,35 @@ __global__ void __launch_bounds__(kBtThreads, 1)
         break;
       }
       tc::tc_fence_after();
-      float sum[64];
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 32) {
+      float sum[32];
+      {
         uint32_t v[32], u[32];
         const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b * kBtAcc + half * 64 + c0);
         tc::tmem_ld_32x32b_x32(base, v);
         tc::tmem_ld_32x32b_x32(base + 128u, u);  // second column half: the cross terms
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) sum[c0 + j] = __uint_as_float(v[j]) + __uint_as_float(u[j]);
+        for (int j = 0; j < 32; ++j) sum[j] = __uint_as_float(v[j]) + __uint_as_float(u[j]);
       }
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&aempty[b]);
       const int64_t prob = 2 * pr + half;
       if (prob < g.batch && i < g.M) {
-        float* cp = g.c + prob * g.stride_c + i;
+        float* cp = g.c + prob * g.stride_c + i + int64_t(c0) * g.ldc;
+        const int nleft = g.N - c0;
         // C is read 16 columns at a time, all loads before any store, so the
         // loads overlap (a store may alias a later load when ldc == 0)
 #pragma unroll
-        for (int j0 = 0; j0 < 64; j0 += 16) {
+        for (int j0 = 0; j0 < 32; j0 += 16) {
           float cv[16];
           if (g.beta != 0.f) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) cv[j] = (j0 + j < g.N) ? cp[int64_t(j0 + j) * g.ldc] : 0.f;
+            for (int j = 0; j < 16; ++j) cv[j] = (j0 + j < nleft) ? cp[int64_t(j0 + j) * g.ldc] : 0.f;
           }
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            if (j0 + j < g.N) {
+            if (j0 + j < nleft) {
               float v = g.alpha * sum[j0 + j];
               if (g.beta != 0.f) v = fmaf(g.beta, cv[j], v);
               cp[int64_t(j0 + j) * g.ldc] = v;
