@@ -130,3 +130,21 @@ def test_gemv_t_warp_per_column_path(sb, torch_cuda, m, n, lda, beta, incy, dtyp
         mask = np.ones(len(y), bool)
         mask[::incy] = False
         np.testing.assert_array_equal(yo[mask], y[mask])
+
+
+@pytest.mark.parametrize("m,n,lda,off", [(1001, 2500, 1001, 0), (1003, 3001, 1005, 1), (2, 2000, 3, 3),
+                                         (4097, 1500, 4099, 2)])
+def test_gemv_t_warp_per_column_misaligned(sb, torch_cuda, m, n, lda, off):
+    """Transposed GEMV with columns that start off a 16-byte boundary (odd lda,
+    A and x at an element offset): each column's head read element-wise, the
+    rest as 16-byte vectors, against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(m + n + lda + off)
+    a = g.uniform(-1, 1, lda * n + off).astype(np.float32)
+    x = g.uniform(-1, 1, m + off).astype(np.float32)
+    y = g.uniform(-1, 1, n).astype(np.float32)
+    ref = oracle.gemv("t", m, n, 0.75, a[off:], lda, x[off:], 1, 0.5, y, 1)
+    ad, xd, yd = to_dev(a, torch), to_dev(x, torch), to_dev(y, torch)
+    blas._gemv(sb, "t", m, n, 0.75, ad[off:], lda, xd[off:], 1, 0.5, yd, 1)
+    np.testing.assert_allclose(to_host(yd), ref, rtol=2e-5, atol=2e-5 * np.abs(ref).max())
