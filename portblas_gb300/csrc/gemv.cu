@@ -29,90 +29,6 @@ struct GemvPolicy {
   }
 };
 
-// ------------------------------------------------- transposed, warp per column --
-// y[j] = alpha * sum_i A[i + j*lda] x[i] + beta * y[j] with one warp per
-// column: lane l reads the 16-byte vectors l, l + 32, ... of the column (and
-// of x, which every warp reads, from L1), kGtwUnroll in flight, then a fixed
-// shuffle tree; no partial sums, no fold, the same order on every run.  The
-// grid is at most one wave (kGtwCtas CTAs of 8 warps per SM, 64 registers,
-// no spills) and column j goes to warp (j / grid) of CTA (j % grid), so the
-// CTAs get the same number of columns to within one.  Taken for x
-// contiguous and, with 16-byte-aligned columns, between a quarter and two
-// columns per warp of the wave; with columns the TMA cannot address
-// (ALIGNED false below) from a quarter column per warp up; otherwise the TMA
-// column sweep
-// (fewer columns leave too few loads in flight, more leave a ragged last
-// round: 16384^2 measured 160 us here against 154 for the sweep).  Not
-// launched early: placed early, its CTAs shared SMs with the GEMV before it
-// and the nine-op step ran 51 us longer, though each op alone was faster.
-// ALIGNED: columns and x 16-byte aligned (x read as 16-byte vectors too);
-// otherwise each column's first elements up to its first 16-byte boundary
-// are read one per lane, the rest of the column as 16-byte vectors, and x
-// one element per lane (x is in L1 after the first columns): a leading
-// dimension that is not a multiple of 16 bytes keeps the vector loads of A.
-constexpr int kGtwUnroll = 4, kGtwCtas = 4;
-
-template <typename T, bool ALIGNED>
-__global__ void __launch_bounds__(kMvThreads, kGtwCtas)
-    gemv_t_warp_cols(GemvPolicy<T> pol, int64_t m, int64_t n, const T* __restrict__ A, int64_t lda,
-                     const T* __restrict__ x) {
-  using V = typename Pack16<T>::V;
-  constexpr int W = Pack16<T>::n;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t step = int64_t(kMvWarps) * gridDim.x;
-  const int64_t first = int64_t(warp) * gridDim.x + blockIdx.x;
-  for (int64_t j = first; j < n; j += step) {
-    const T* col = A + j * lda;
-    T acc = T(0);
-    int64_t head = 0;  // elements before the column's first 16-byte boundary
-    if (!ALIGNED) {
-      head = int64_t(((16 - (reinterpret_cast<uintptr_t>(col) & 15)) & 15) / sizeof(T));
-      if (head > m) head = m;
-      if (lane < head) acc = col[lane] * x[lane];
-    }
-    const V* av = reinterpret_cast<const V*>(col + head);
-    const T* xh = x + head;
-    const int64_t nv = (m - head) / W;  // whole vectors after the head
-    int64_t v = lane;
-    for (; v + 32 * (kGtwUnroll - 1) < nv; v += 32 * kGtwUnroll) {
-      V a[kGtwUnroll];
-#pragma unroll
-      for (int u = 0; u < kGtwUnroll; ++u) a[u] = __ldcs(av + v + 32 * u);
-      if (ALIGNED) {
-        V b[kGtwUnroll];
-#pragma unroll
-        for (int u = 0; u < kGtwUnroll; ++u) b[u] = __ldg(reinterpret_cast<const V*>(xh) + v + 32 * u);
-#pragma unroll
-        for (int u = 0; u < kGtwUnroll; ++u) {
-          T ae[W], be[W];
-          Pack16<T>::get(a[u], ae);
-          Pack16<T>::get(b[u], be);
-#pragma unroll
-          for (int e = 0; e < W; ++e) acc = fma(ae[e], be[e], acc);
-        }
-      } else {
-#pragma unroll
-        for (int u = 0; u < kGtwUnroll; ++u) {
-          T ae[W];
-          Pack16<T>::get(a[u], ae);
-#pragma unroll
-          for (int e = 0; e < W; ++e) acc = fma(ae[e], __ldg(xh + (v + 32 * u) * W + e), acc);
-        }
-      }
-    }
-    for (; v < nv; v += 32) {
-      T ae[W];
-      Pack16<T>::get(__ldcs(av + v), ae);
-#pragma unroll
-      for (int e = 0; e < W; ++e) acc = fma(ae[e], __ldg(xh + v * W + e), acc);
-    }
-    for (int64_t i = head + nv * W + lane; i < m; i += 32) acc = fma(col[i], x[i], acc);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) pol.finish(acc, j);
-  }
-}
-
 template <typename T>
 gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T alpha, const T* a, int64_t lda,
                           const T* x, int64_t incx, T beta, T* y, int64_t incy) {
@@ -148,22 +64,15 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
     return after_launch("gemv_n");
   }
   {
-    // one column per warp where that fits in one wave, else the full wave
-    const int64_t slots = int64_t(kGtwCtas) * h->sm_count, warps = slots * kMvWarps;
-    const int64_t want = cdiv(n, int64_t(kMvWarps));
-    const int64_t grid = want < slots ? want : slots;
-    // aligned A: the warp kernel up to two columns per warp (the TMA sweep
-    // beyond); A the TMA cannot address (unaligned lda): the warp kernel at
-    // any width, against the element-wise sweep otherwise
-    if (incx == 1 && m > 0 && 4 * n >= warps) {
-      if (vec && aligned16(x) && n <= 2 * warps) {
-        gemv_t_warp_cols<T, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, m, n, a, lda, x);
-        return after_launch("gemv_t_warp_cols");
-      }
-      if (!vec) {
-        gemv_t_warp_cols<T, false><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, m, n, a, lda, x);
-        return after_launch("gemv_t_warp_cols");
-      }
+    // one warp per column (cols_warp in matvec.cuh): aligned columns up to
+    // two per warp of the wave (16384^2 measured 160 us there against 154
+    // for the TMA sweep, whose full-width rounds end evenly), columns the TMA
+    // cannot address at any width (8191^2: 49 us against 100 for the
+    // element-wise sweep).  It is not launched early: placed early, its CTAs
+    // shared SMs with the GEMV before it and the nine-op step ran 51 us longer.
+    if (incx == 1) {
+      gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
+      if (try_cols_warp<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, x, true, &st)) return st;
     }
     gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
     if (try_cols_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;

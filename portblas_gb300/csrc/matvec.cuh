@@ -38,6 +38,109 @@ struct Pack16<double> {
 constexpr int kMvThreads = 256;
 constexpr int kMvWarps = kMvThreads / 32;
 
+// ------------------------------------------------------- warp per column --
+// out(j) = fold over i of pol.add(A[i + j*lda], x[i]) with one warp per
+// column j: lane l reads the 16-byte vectors l, l + 32, ... of the column
+// (kCwUnroll in flight) and, with HAS_X, the matching x through L1, then a
+// fixed shuffle tree; no partial sums, no fold across CTAs, the same order on
+// every run.  The grid is at most one wave (kCwCtas CTAs of 8 warps per SM,
+// 64 registers) and column j goes to warp j / grid of CTA j % grid, so the
+// CTAs get the same number of columns to within one.  ALIGNED: the columns
+// (and x) are 16-byte aligned; otherwise each column's elements before its
+// first 16-byte boundary are read one per lane, the rest as 16-byte vectors,
+// and x one element per lane, so a leading dimension TMA cannot address
+// keeps the vector loads of A.
+constexpr int kCwUnroll = 4, kCwCtas = 4;
+
+template <class P, typename T, bool HAS_X, bool ALIGNED>
+__global__ void __launch_bounds__(kMvThreads, kCwCtas)
+    cols_warp(P pol, int64_t m, int64_t n, const T* __restrict__ A, int64_t lda, const T* __restrict__ x) {
+  using V = typename Pack16<T>::V;
+  using Acc = typename P::Acc;
+  constexpr int W = Pack16<T>::n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t step = int64_t(kMvWarps) * gridDim.x;
+  const int64_t first = int64_t(warp) * gridDim.x + blockIdx.x;
+  for (int64_t j = first; j < n; j += step) {
+    const T* col = A + j * lda;
+    Acc acc = pol.init();
+    int64_t head = 0;  // elements before the column's first 16-byte boundary
+    if (!ALIGNED) {
+      head = int64_t(((16 - (reinterpret_cast<uintptr_t>(col) & 15)) & 15) / sizeof(T));
+      if (head > m) head = m;
+      if (lane < head) pol.add(acc, col[lane], HAS_X ? x[lane] : T(1));
+    }
+    const V* av = reinterpret_cast<const V*>(col + head);
+    const T* xh = HAS_X ? x + head : x;
+    const int64_t nv = (m - head) / W;  // whole vectors after the head
+    int64_t v = lane;
+    for (; v + 32 * (kCwUnroll - 1) < nv; v += 32 * kCwUnroll) {
+      V a[kCwUnroll];
+#pragma unroll
+      for (int u = 0; u < kCwUnroll; ++u) a[u] = __ldcs(av + v + 32 * u);
+      if (HAS_X && ALIGNED) {
+        V b[kCwUnroll];
+#pragma unroll
+        for (int u = 0; u < kCwUnroll; ++u) b[u] = __ldg(reinterpret_cast<const V*>(xh) + v + 32 * u);
+#pragma unroll
+        for (int u = 0; u < kCwUnroll; ++u) {
+          T ae[W], be[W];
+          Pack16<T>::get(a[u], ae);
+          Pack16<T>::get(b[u], be);
+#pragma unroll
+          for (int e = 0; e < W; ++e) pol.add(acc, ae[e], be[e]);
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < kCwUnroll; ++u) {
+          T ae[W];
+          Pack16<T>::get(a[u], ae);
+#pragma unroll
+          for (int e = 0; e < W; ++e) pol.add(acc, ae[e], HAS_X ? __ldg(xh + (v + 32 * u) * W + e) : T(1));
+        }
+      }
+    }
+    for (; v < nv; v += 32) {
+      T ae[W];
+      Pack16<T>::get(__ldcs(av + v), ae);
+#pragma unroll
+      for (int e = 0; e < W; ++e) pol.add(acc, ae[e], HAS_X ? __ldg(xh + v * W + e) : T(1));
+    }
+    for (int64_t i = head + nv * W + lane; i < m; i += 32) pol.add(acc, col[i], HAS_X ? x[i] : T(1));
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const Acc o = pol.shfl_down(acc, off);
+      pol.merge(acc, o);
+    }
+    if (lane == 0) pol.finish(acc, j);
+  }
+}
+
+// Launches cols_warp when it applies and returns true (status in *st):
+// x contiguous (or no x), at least a quarter column per warp of the wave,
+// and either 16-byte-aligned columns and x with at most two columns per warp
+// (when aligned_ok), or columns TMA cannot address at any width.
+template <class P, typename T, bool HAS_X>
+inline bool try_cols_warp(gbblas_handle_t h, const P& pol, int64_t m, int64_t n, const T* A, int64_t lda,
+                          const T* x, bool aligned_ok, gbblas_status_t* st) {
+  constexpr int W = 16 / int(sizeof(T));
+  const int64_t slots = int64_t(kCwCtas) * h->sm_count, warps = slots * kMvWarps;
+  if (m <= 0 || 4 * n < warps) return false;
+  const int64_t want = (n + kMvWarps - 1) / kMvWarps;
+  const unsigned grid = unsigned(want < slots ? want : slots);
+  const bool vec_a = lda % W == 0 && aligned16(A);
+  if (vec_a && (!HAS_X || aligned16(x))) {
+    if (!aligned_ok || n > 2 * warps) return false;
+    cols_warp<P, T, HAS_X, true><<<grid, kMvThreads, 0, h->stream>>>(pol, m, n, A, lda, x);
+  } else if (!vec_a) {
+    cols_warp<P, T, HAS_X, false><<<grid, kMvThreads, 0, h->stream>>>(pol, m, n, A, lda, x);
+  } else {
+    return false;  // aligned columns with an unaligned x: the TMA sweep
+  }
+  *st = after_launch("cols_warp");
+  return true;
+}
+
 // ------------------------------------------------------------- rows sweep --
 // CTA = 8 warps over a block of 32*RPT rows; warp w takes columns
 // c0+w, c0+w+8, ... of its split; the 8 warp partials fold in warp order.

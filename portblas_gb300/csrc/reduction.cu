@@ -124,6 +124,10 @@ gbblas_status_t reduction_op(gbblas_handle_t h, int dim, const T* in, int64_t ld
     gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
     if (try_cols_sweep_tma<P, T, false>(h, pol, rows, cols, in, ld, static_cast<const T*>(nullptr), 0, &st))
       return st;
+    // columns TMA cannot address: one warp per column with 16-byte loads
+    // after each column's head (cols_warp in matvec.cuh)
+    if (try_cols_warp<P, T, false>(h, pol, rows, cols, in, ld, static_cast<const T*>(nullptr), false, &st))
+      return st;
   }
   SweepPlan p = plan_cols(rows, cols, h->sm_count, sizeof(T));
   const int64_t chunk_cols = int64_t(kMaxTickets) * p.cols_per_cta;
