@@ -144,8 +144,12 @@ inline bool try_cols_warp(gbblas_handle_t h, const P& pol, int64_t m, int64_t n,
 // ------------------------------------------------------------- rows sweep --
 // CTA = 8 warps over a block of 32*RPT rows; warp w takes columns
 // c0+w, c0+w+8, ... of its split; the 8 warp partials fold in warp order.
+// VEC: lane l owns rows RPT*l .. RPT*l + RPT-1 (one 16-byte load per
+// column); otherwise rows l, l + 32, ..., so each element-wise load of a
+// warp covers 32 consecutive rows (one 128-byte line instead of a 512-byte
+// span at a 16-byte stride).
 template <class P, typename T, bool VEC, bool HAS_X>
-__global__ void __launch_bounds__(kMvThreads, 8)
+__global__ void __launch_bounds__(kMvThreads, 4)
     rows_sweep(P pol, int64_t M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
                int64_t incx, int64_t cols_per_split, typename P::Acc* __restrict__ partials,
                unsigned int* __restrict__ tickets) {
@@ -156,21 +160,23 @@ __global__ void __launch_bounds__(kMvThreads, 8)
   __shared__ bool is_last;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t rblock = blockIdx.x;
-  const int64_t row0 = rblock * WR + lane * RPT;
+  // offset (within the block) of the r-th row this lane owns
+  auto rof = [&](int r) { return VEC ? lane * RPT + r : r * 32 + lane; };
+  const int64_t row0 = rblock * WR + rof(0);
   const int64_t c0 = int64_t(blockIdx.y) * cols_per_split;
   const int64_t c1 = min(N, c0 + cols_per_split);
   Acc acc[RPT];
 #pragma unroll
   for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
   const bool full = VEC && (row0 + RPT <= M);
-  const T* Ap = A + row0;
+  const T* Ab = A + rblock * WR;
 
   auto load_col = [&](int64_t j, T* v) {
     if (full) {
-      Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(Ap + j * lda)), v);
+      Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(Ab + rof(0) + j * lda)), v);
     } else {
 #pragma unroll
-      for (int r = 0; r < RPT; ++r) v[r] = (row0 + r < M) ? Ap[j * lda + r] : T(0);
+      for (int r = 0; r < RPT; ++r) v[r] = (rblock * WR + rof(r) < M) ? Ab[j * lda + rof(r)] : T(0);
     }
   };
 
@@ -197,7 +203,7 @@ __global__ void __launch_bounds__(kMvThreads, 8)
     for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[r], xv);
   }
 #pragma unroll
-  for (int r = 0; r < RPT; ++r) red[warp][lane * RPT + r] = acc[r];
+  for (int r = 0; r < RPT; ++r) red[warp][rof(r)] = acc[r];
   __syncthreads();
   const int t = threadIdx.x;
   const int64_t row = rblock * WR + t;
@@ -320,7 +326,7 @@ inline SweepPlan plan_rows(int64_t M, int64_t N, int sm_count, int elem_bytes) {
   const int64_t WR = 32 * (16 / elem_bytes);
   SweepPlan p;
   p.tiles = cdiv(M > 0 ? M : 1, WR);
-  const int64_t target = int64_t(sm_count) * 8;
+  const int64_t target = int64_t(sm_count) * 4;  // one wave of rows_sweep (4 CTAs per SM)
   int64_t split = cdiv(target, p.tiles);
   const int64_t max_split = cdiv(N > 0 ? N : 1, 64);
   if (split > max_split) split = max_split;
