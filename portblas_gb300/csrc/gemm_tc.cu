@@ -541,6 +541,220 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
   }
 }
 
+// ------------------------------------------- CTA-pair tiles of 256 x 256 --
+// The same schedule as the 256 x 128 pair kernel above with N = 256 per
+// cluster: each CTA loads its 128 rows of A and 128 rows (its half) of B per
+// stage (64 KB, three stages), the even CTA issues tcgen05.mma.cta_group::2
+// M256 N256 K16, so each MMA does twice the work for the same A read; two
+// TMEM accumulators of 256 columns; sixteen epilogue warps per CTA (two
+// warps' worth of columns per TMEM lane quarter... four column groups of 64).
+// Used where the 256 x 256 tiles give every resident cluster several rounds.
+constexpr int kPair2BN = 256, kPair2BHalf = kPair2BN / 2;
+constexpr int kPair2EpiWarps = 16, kPair2Threads = 32 * (2 + kPair2EpiWarps);
+constexpr int kPair2Acc = 2;
+
+template <int STAGES>
+struct Pair2Cfg {
+  static constexpr int P = 2;
+  static constexpr int A_TILE = kTcBM * kTcBK * 2;        // 16 KB
+  static constexpr int B_TILE = kPair2BHalf * kTcBK * 2;  // 16 KB
+  static constexpr int STAGE = P * (A_TILE + B_TILE);     // 64 KB
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static constexpr int TMEM_COLS = kPair2Acc * kPair2BN;  // all 512 columns
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+template <int STAGES>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
+    gemm_split_bf16_pair256_kernel(const __grid_constant__ CUtensorMap tma_a,
+                                   const __grid_constant__ CUtensorMap tma_b, int M, int N, int nk, int tiles,
+                                   float alpha, float beta, float* __restrict__ C, int64_t ldc, int64_t stride_c,
+                                   int* __restrict__ err) {
+  using Cfg = Pair2Cfg<STAGES>;
+  constexpr int P = Cfg::P;
+  const uint32_t rank = tc::cluster_ctarank();  // 0: issues the MMAs
+  const int cid = int(blockIdx.x >> 1), clusters = int(gridDim.x >> 1);
+  const int mp_count = (M + 2 * kTcBM - 1) / (2 * kTcBM), nt_count = (N + kPair2BN - 1) / kPair2BN;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* tiles_smem = smem;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * Cfg::STAGE);  // even CTA: both CTAs' bytes
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;      // [kPair2Acc]
+  uint64_t* tempty = tfull + kPair2Acc;  // [kPair2Acc] even CTA: drained by both CTAs' epilogues
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + kPair2Acc);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < kPair2Acc; ++b) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], 2 * kPair2EpiWarps);  // the epilogue warps of both CTAs
+    }
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc_pair(tmem_slot, Cfg::TMEM_COLS);
+    tc::tmem_relinquish_pair();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  pdl_wait();  // the operand terms (and C) are written by earlier kernels on the stream
+
+  if (warp == 0) {
+    if (lane == 0) {
+      tc::tma_prefetch_desc(&tma_a);
+      tc::tma_prefetch_desc(&tma_b);
+      const uint32_t full0 = tc::mapa_shared(tc::smem_u32(full), 0);
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = cid; t < tiles && ok; t += clusters) {
+        int bz, mp, nt;
+        pair_tile(t, mp_count, nt_count, bz, mp, nt);
+        const int m0 = mp * (2 * kTcBM) + int(rank) * kTcBM, n0 = nt * kPair2BN + int(rank) * kPair2BHalf;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int s = int(it % STAGES);
+          if (!tc::mbar_wait(&empty[s], ((it / STAGES) & 1) ^ 1)) {
+            atomicExch(err, kErrPairProducer);
+            ok = false;
+            break;
+          }
+          if (rank == 0) tc::mbar_arrive_expect_tx(&full[s], 2 * Cfg::STAGE);
+          const uint32_t bar = full0 + uint32_t(s) * 8u;
+          uint8_t* st = tiles_smem + s * Cfg::STAGE;
+#pragma unroll
+          for (int p = 0; p < P; ++p)
+            tc::tma_load_3d_pair(st + p * Cfg::A_TILE, &tma_a, bar, kb * kTcBK, m0, bz * P + p);
+#pragma unroll
+          for (int p = 0; p < P; ++p)
+            tc::tma_load_3d_pair(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, bar, kb * kTcBK, n0, bz * P + p);
+        }
+      }
+      if (rank == 0)
+        for (uint32_t j = it > uint32_t(STAGES) ? it - STAGES : 0u; j < it; ++j)
+          if (!tc::mbar_wait(&full[j % STAGES], (j / STAGES) & 1)) {
+            atomicExch(err, kErrPairDrain);
+            break;
+          }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && rank == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * kTcBM, kPair2BN);
+      uint32_t it = 0, g = 0;
+      bool ok = true;
+      for (int t = cid; t < tiles && ok; t += clusters) {
+        for (int c = 0; c < nchunks && ok; ++c, ++g) {
+          const int b = int(g % kPair2Acc);
+          if (!tc::mbar_wait(&tempty[b], ((g / kPair2Acc) & 1) ^ 1)) {
+            atomicExch(err, kErrPairMma);
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t acc = tmem + uint32_t(b * kPair2BN);
+          const int kb1 = min(nk, (c + 1) * kTcChunk);
+          for (int kb = c * kTcChunk; kb < kb1; ++kb, ++it) {
+            const int s = int(it % STAGES);
+            if (!tc::mbar_wait(&full[s], (it / STAGES) & 1)) {
+              atomicExch(err, kErrPairMma);
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint8_t* st = tiles_smem + s * Cfg::STAGE;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              int pa, pb;
+              term_pair(q, pa, pb);
+              const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
+              const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
+#pragma unroll
+              for (int j = 0; j < kTcBK / 16; ++j)
+                tc::mma_bf16_pair(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+            }
+            tc::mma_commit_pair(&empty[s], 0x3);
+          }
+          if (ok) tc::mma_commit_pair(&tfull[b], 0x3);
+        }
+      }
+    }
+  } else {
+    // epilogue warps 2..17: warp w owns TMEM lanes [32*(w%4), +32) (one row
+    // of this CTA's 128 per thread) and columns [64*cg, +64), cg = (w - 2) / 4
+    const int q = warp & 3, cg = (warp - 2) >> 2;
+    const int row = q * 32 + lane;
+    const uint32_t tempty0 = tc::mapa_shared(tc::smem_u32(tempty), 0);
+    uint32_t g = 0;
+    bool ok = true;
+    for (int t = cid; t < tiles && ok; t += clusters) {
+      int bz, mp, nt;
+      pair_tile(t, mp_count, nt_count, bz, mp, nt);
+      const int gm = mp * (2 * kTcBM) + int(rank) * kTcBM + row, nb = nt * kPair2BN + cg * 64;
+      float sum[64];
+#pragma unroll
+      for (int i = 0; i < 64; ++i) sum[i] = 0.f;
+      for (int c = 0; c < nchunks; ++c, ++g) {
+        const int b = int(g % kPair2Acc);
+        if (!tc::mbar_wait(&tfull[b], (g / kPair2Acc) & 1)) {
+          if (lane == 0) atomicExch(err, kErrPairEpilogue);
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t base = tmem + (uint32_t(q * 32) << 16) + uint32_t(b * kPair2BN + cg * 64);
+        // 8 columns per wait: the 64 running sums and the loaded values fit
+        // the 96 registers a thread of an 18-warp CTA gets
+#pragma unroll
+        for (int hh = 0; hh < 8; ++hh) {
+          uint32_t r0[8];
+          tc::tmem_ld_32x32b_x8(base + uint32_t(8 * hh), r0);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 8; ++i) sum[8 * hh + i] += __uint_as_float(r0[i]);
+        }
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive_cluster(tempty0 + uint32_t(b) * 8u);
+      }
+      if (ok && gm < M) {
+        float* rowp = C + int64_t(bz) * stride_c + int64_t(gm);
+#pragma unroll
+        for (int g0 = 0; g0 < 64; g0 += 8) {
+          float cv[8];
+          if (beta != 0.f) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) cv[i] = (nb + g0 + i < N) ? rowp[int64_t(nb + g0 + i) * ldc] : 0.f;
+          }
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int gn = nb + g0 + i;
+            if (gn < N) {
+              float v = alpha * sum[g0 + i];
+              if (beta != 0.f) v = fmaf(beta, cv[i], v);
+              rowp[int64_t(gn) * ldc] = v;
+            }
+          }
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc_pair(tmem, Cfg::TMEM_COLS);
+  }
+}
+
 // ------------------------------------------------------------ split pass --
 // out[p][r][k] (k < Kp) = term p of X(r, k); X(r, k) = X[r*sr + k*sk]; zero
 // for k >= K; Kp is a multiple of 64.  One CTA per 64 x 64 tile, 256
@@ -748,9 +962,48 @@ static gbblas_status_t launch_tc_pair(gbblas_handle_t h, const CUtensorMap& ta, 
   return after_launch("gemm_split_bf16_pair");
 }
 
+// 256 x 256 tiles on CTA pairs (x3, no split-K): a persistent grid of the
+// clusters that can be resident at once.
+static gbblas_status_t launch_tc_pair256(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb,
+                                         int64_t M, int64_t N, int64_t nk, int64_t batch, float alpha, float beta,
+                                         float* C, int64_t ldc, int64_t stride_c) {
+  constexpr int STAGES = 3;
+  using Cfg = Pair2Cfg<STAGES>;
+  auto* kern = gemm_split_bf16_pair256_kernel<STAGES>;
+  static std::atomic<uint64_t> attr{0};
+  GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(kern), Cfg::SMEM, h->device));
+  const int64_t tiles = cdiv(M, 2 * kTcBM) * cdiv(N, kPair2BN) * batch;
+  if (tiles > INT32_MAX / 2) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: too many tiles");
+  static std::atomic<int> resident[64];
+  int clusters = (h->device >= 0 && h->device < 64) ? resident[h->device].load(std::memory_order_acquire) : 0;
+  if (clusters <= 0) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * unsigned(h->sm_count / 2), 1, 1);
+    cfg.blockDim = dim3(kPair2Threads, 1, 1);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = h->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&clusters, reinterpret_cast<const void*>(kern), &cfg));
+    if (clusters < 1) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: no CTA pair can be resident");
+    if (h->device >= 0 && h->device < 64) resident[h->device].store(clusters, std::memory_order_release);
+  }
+  const int64_t grid_clusters = std::min<int64_t>(tiles, clusters);
+  const cudaError_t le = launch_pdl(true, kern, dim3(unsigned(2 * grid_clusters)), dim3(kPair2Threads), Cfg::SMEM,
+                                    h->stream, ta, tb, int(M), int(N), int(nk), int(tiles), alpha, beta, C, ldc,
+                                    stride_c, h->dev_error);
+  if (le != cudaSuccess) return cuda_fail(le, "gemm_split_bf16_pair256");
+  return after_launch("gemm_split_bf16_pair256");
+}
+
 template <int BN, int P>
 static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& g, int split, int raster_m,
-                                      bool pair = false) {
+                                      int pair = 0) {
   constexpr int STAGES = (P * (kTcBM + BN) * kTcBK * 2) <= 56 * 1024 ? 4 : ((P * (kTcBM + BN) * kTcBK * 2) <= 72 * 1024 ? 3 : 2);
   const int64_t M = g.m, N = g.n, K = g.k, B = g.batch;
   const int64_t Kp = cdiv(K, kTcBK) * kTcBK;
@@ -774,9 +1027,13 @@ static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& 
                          split_operand(g.b, g.tb ? 1 : g.ldb, g.tb ? g.ldb : 1, N, g.stride_b, bt), K, Kp, B));
   CUtensorMap ma, mb;
   GB_TRY(make_term_map(&ma, at, M, Kp, P * B, kTcBM));
-  if (pair && P == 2 && split == 1) {
+  if (pair == 1 && P == 2 && split == 1) {
     GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, kPairBHalf));
     return launch_tc_pair(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
+  }
+  if (pair == 2 && P == 2 && split == 1) {
+    GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, kPair2BHalf));
+    return launch_tc_pair256(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
   }
   GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, BN));
   if (split == 1)
@@ -817,8 +1074,12 @@ static bool pair_tiles_enabled() {
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
   const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
-  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled())
-    return split_gemm_run<128, 2>(h, g, 1, 0, true);
+  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) {
+    // 256 x 256 cluster tiles when every resident cluster gets at least
+    // eight, else 256 x 128
+    const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
+    return split_gemm_run<128, 2>(h, g, 1, 0, t256 >= 8 * (sm / 2) ? 2 : 1);
+  }
   if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 2);
   const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
   int64_t split = 1;
