@@ -64,12 +64,14 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
     return after_launch("gemv_n");
   }
   {
-    // one warp per column (cols_warp in matvec.cuh): aligned columns up to
-    // two per warp of the wave (16384^2 measured 160 us there against 154
-    // for the TMA sweep, whose full-width rounds end evenly), columns the TMA
-    // cannot address at any width (8191^2: 49 us against 100 for the
-    // element-wise sweep).  It is not launched early: placed early, its CTAs
-    // shared SMs with the GEMV before it and the nine-op step ran 51 us longer.
+    // aligned columns up to two per warp of the wave: a CTA per column
+    // group, its warps over equal row ranges (cols_cta in matvec.cuh; 8192^2
+    // 45.0 -> 42.2 us against one warp per column, whose warps got one or
+    // two columns; the TMA sweep's rounds end evenly only at full widths such
+    // as 16384^2); columns the TMA cannot address at any width: one warp per
+    // column (cols_warp; 8191^2: 49 us against 100 for the element-wise
+    // sweep).  Neither is launched early: placed early, the CTAs shared SMs
+    // with the GEMV before it and the nine-op step ran 51 us longer.
     if (incx == 1) {
       gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
       if (try_cols_warp<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, x, true, &st)) return st;

@@ -116,10 +116,83 @@ __global__ void __launch_bounds__(kMvThreads, kCwCtas)
   }
 }
 
-// Launches cols_warp when it applies and returns true (status in *st):
-// x contiguous (or no x), at least a quarter column per warp of the wave,
-// and either 16-byte-aligned columns and x with at most two columns per warp
-// (when aligned_ok), or columns TMA cannot address at any width.
+// ----------------------------------------------- CTA per column group --
+// out(j) = fold over i of pol.add(A[i + j*lda], x[i]) for 16-byte-aligned
+// columns and x: CTA b takes columns b, b + grid, ... (the CTAs' counts
+// differ by at most one) and, for each, its eight warps take equal
+// contiguous row ranges (whole 32-vector rounds), so every warp of the wave
+// streams the same number of bytes; each warp folds its range with a fixed
+// shuffle tree and the CTA's thread t folds column t's eight warp partials
+// in warp order (deterministic).  One warp per column leaves the wave
+// uneven when the columns are not a whole number per warp (8192 columns on
+// 4864 warps: 1536 warps with one column, 3328 with two).
+constexpr int kCcMaxCols = 16;
+static_assert(2 * kMvWarps <= kCcMaxCols && kCcMaxCols <= kMvThreads, "cols_cta column budget");
+
+template <class P, typename T>
+__global__ void __launch_bounds__(kMvThreads, kCwCtas)
+    cols_cta(P pol, int64_t m, int64_t n, const T* __restrict__ A, int64_t lda, const T* __restrict__ x) {
+  using V = typename Pack16<T>::V;
+  using Acc = typename P::Acc;
+  constexpr int W = Pack16<T>::n;
+  __shared__ Acc red[kCcMaxCols][kMvWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nv = m / W;  // whole vectors per column; the last warp adds the m % W tail rows
+  const int64_t per = (((nv + kMvWarps - 1) / kMvWarps) + 31) / 32 * 32;
+  const int64_t v0 = int64_t(warp) * per, v1 = v0 + per < nv ? v0 + per : nv;
+  const V* xv = reinterpret_cast<const V*>(x);
+  int cols = 0;
+  for (int64_t j = blockIdx.x; j < n && cols < kCcMaxCols; j += gridDim.x, ++cols) {
+    const V* av = reinterpret_cast<const V*>(A + j * lda);
+    Acc acc = pol.init();
+    int64_t v = v0 + lane;
+    for (; v + 32 * (kCwUnroll - 1) < v1; v += 32 * kCwUnroll) {
+      V a[kCwUnroll], b[kCwUnroll];
+#pragma unroll
+      for (int u = 0; u < kCwUnroll; ++u) a[u] = __ldcs(av + v + 32 * u);
+#pragma unroll
+      for (int u = 0; u < kCwUnroll; ++u) b[u] = __ldg(xv + v + 32 * u);
+#pragma unroll
+      for (int u = 0; u < kCwUnroll; ++u) {
+        T ae[W], be[W];
+        Pack16<T>::get(a[u], ae);
+        Pack16<T>::get(b[u], be);
+#pragma unroll
+        for (int e = 0; e < W; ++e) pol.add(acc, ae[e], be[e]);
+      }
+    }
+    for (; v < v1; v += 32) {
+      T ae[W], be[W];
+      Pack16<T>::get(__ldcs(av + v), ae);
+      Pack16<T>::get(__ldg(xv + v), be);
+#pragma unroll
+      for (int e = 0; e < W; ++e) pol.add(acc, ae[e], be[e]);
+    }
+    if (warp == kMvWarps - 1 && lane < m - nv * W) {
+      const T* col = A + j * lda;
+      pol.add(acc, col[nv * W + lane], x[nv * W + lane]);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const Acc o = pol.shfl_down(acc, off);
+      pol.merge(acc, o);
+    }
+    if (lane == 0) red[cols][warp] = acc;
+  }
+  __syncthreads();
+  if (int(threadIdx.x) < cols) {
+    Acc acc = red[threadIdx.x][0];
+#pragma unroll
+    for (int w = 1; w < kMvWarps; ++w) pol.merge(acc, red[threadIdx.x][w]);
+    pol.finish(acc, int64_t(blockIdx.x) + int64_t(threadIdx.x) * gridDim.x);
+  }
+}
+
+// Launches cols_cta (16-byte-aligned columns and x) or cols_warp when one
+// applies and returns true (status in *st): x contiguous (or no x), at least
+// a quarter column per warp of the wave, and either aligned columns and x
+// with at most two columns per warp (when aligned_ok), or columns TMA cannot
+// address at any width.
 template <class P, typename T, bool HAS_X>
 inline bool try_cols_warp(gbblas_handle_t h, const P& pol, int64_t m, int64_t n, const T* A, int64_t lda,
                           const T* x, bool aligned_ok, gbblas_status_t* st) {
@@ -131,7 +204,13 @@ inline bool try_cols_warp(gbblas_handle_t h, const P& pol, int64_t m, int64_t n,
   const bool vec_a = lda % W == 0 && aligned16(A);
   if (vec_a && (!HAS_X || aligned16(x))) {
     if (!aligned_ok || n > 2 * warps) return false;
-    cols_warp<P, T, HAS_X, true><<<grid, kMvThreads, 0, h->stream>>>(pol, m, n, A, lda, x);
+    if (HAS_X) {
+      // at most 2 * kMvWarps <= kCcMaxCols columns per CTA
+      const unsigned cgrid = unsigned(n < slots ? n : slots);
+      cols_cta<P, T><<<cgrid, kMvThreads, 0, h->stream>>>(pol, m, n, A, lda, x);
+    } else {
+      cols_warp<P, T, HAS_X, true><<<grid, kMvThreads, 0, h->stream>>>(pol, m, n, A, lda, x);
+    }
   } else if (!vec_a) {
     cols_warp<P, T, HAS_X, false><<<grid, kMvThreads, 0, h->stream>>>(pol, m, n, A, lda, x);
   } else {

@@ -105,13 +105,15 @@ def test_gemv_tma_stream_path(sb, torch_cuda, trans, m, n, lda, beta):
     np.testing.assert_array_equal(yo[mask], y[mask])
 
 
-@pytest.mark.parametrize("m,n,lda", [(1001, 2500, 1004), (3, 3000, 4), (4096, 9728, 4096), (130, 1300, 132)])
+@pytest.mark.parametrize("m,n,lda", [(1001, 2500, 1004), (3, 3000, 4), (4096, 9728, 4096), (130, 1300, 132),
+                                     (5, 1216, 8), (8193, 4865, 8196)])
 @pytest.mark.parametrize("beta,incy", [(0.0, 1), (0.5, 3)])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_gemv_t_warp_per_column_path(sb, torch_cuda, m, n, lda, beta, incy, dtype):
     """Transposed GEMV over many columns with contiguous x and 16-byte-aligned
-    columns (one warp per column): ragged column lengths (vector part plus
-    scalar tail, or the tail alone), up to two columns per warp, strided y;
+    columns (a CTA per group of columns, its warps over equal row ranges):
+    ragged column lengths (vector part plus scalar tail, or the tail alone,
+    fewer vectors than warps), one to sixteen columns per CTA, strided y;
     every entry against the oracle and y's gaps untouched."""
     torch = torch_cuda
     from portblas_gb300 import blas
