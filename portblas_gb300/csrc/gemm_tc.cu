@@ -544,34 +544,47 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
 // ------------------------------------------- CTA-pair tiles of 256 x 256 --
 // The same schedule as the 256 x 128 pair kernel above with N = 256 per
 // cluster: each CTA loads its 128 rows of A and 128 rows (its half) of B per
-// stage (64 KB, three stages), the even CTA issues tcgen05.mma.cta_group::2
-// M256 N256 K16, so each MMA does twice the work for the same A read; two
-// TMEM accumulators of 256 columns; sixteen epilogue warps per CTA (two
-// warps' worth of columns per TMEM lane quarter... four column groups of 64).
-// Used where the 256 x 256 tiles give every resident cluster several rounds.
+// term and stage (x3: 64 KB, three stages; x6: 96 KB, two stages), the even
+// CTA issues tcgen05.mma.cta_group::2 M256 N256 K16, so each MMA does twice
+// the work for the same A read; every term product of a TMEM chunk goes into
+// one accumulator (two of 256 columns, so the MMAs of the next chunk run
+// while the epilogue promotes this one); sixteen epilogue warps per CTA, four
+// per TMEM lane quarter, each with 64 of the 256 columns.  Used where the
+// 256 x 256 tiles give every resident cluster at least eight rounds.
 constexpr int kPair2BN = 256, kPair2BHalf = kPair2BN / 2;
 constexpr int kPair2EpiWarps = 16, kPair2Threads = 32 * (2 + kPair2EpiWarps);
 constexpr int kPair2Acc = 2;
 
-template <int STAGES>
+template <int P_, int STAGES>
 struct Pair2Cfg {
-  static constexpr int P = 2;
+  static constexpr int P = P_;
   static constexpr int A_TILE = kTcBM * kTcBK * 2;        // 16 KB
   static constexpr int B_TILE = kPair2BHalf * kTcBK * 2;  // 16 KB
-  static constexpr int STAGE = P * (A_TILE + B_TILE);     // 64 KB
+  static constexpr int STAGE = P * (A_TILE + B_TILE);     // 64 KB (x3) / 96 KB (x6)
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
   static constexpr int TMEM_COLS = kPair2Acc * kPair2BN;  // all 512 columns
+  // term products per k-block: x3 (0,0) (0,1) (1,0); x6 adds (1,1) (0,2) (2,0)
+  static constexpr int NPROD = P == 2 ? 3 : 6;
+  // k-blocks per TMEM chunk: every product of the chunk goes into the one
+  // accumulator, so x6 (six MMAs per K16 step) promotes twice as often
+  static constexpr int CHUNK = P == 2 ? kTcChunk : kTcChunk / 2;
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
-template <int STAGES>
+// (a-term, b-term) of product q, largest first
+__device__ __forceinline__ void term_pair6(int q, int& pa, int& pb) {
+  constexpr int kA[6] = {0, 0, 1, 1, 0, 2}, kB[6] = {0, 1, 0, 1, 2, 0};
+  pa = kA[q];
+  pb = kB[q];
+}
+
+template <int P, int STAGES>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
     gemm_split_bf16_pair256_kernel(const __grid_constant__ CUtensorMap tma_a,
                                    const __grid_constant__ CUtensorMap tma_b, int M, int N, int nk, int tiles,
                                    float alpha, float beta, float* __restrict__ C, int64_t ldc, int64_t stride_c,
                                    int* __restrict__ err) {
-  using Cfg = Pair2Cfg<STAGES>;
-  constexpr int P = Cfg::P;
+  using Cfg = Pair2Cfg<P, STAGES>;
   const uint32_t rank = tc::cluster_ctarank();  // 0: issues the MMAs
   const int cid = int(blockIdx.x >> 1), clusters = int(gridDim.x >> 1);
   const int mp_count = (M + 2 * kTcBM - 1) / (2 * kTcBM), nt_count = (N + kPair2BN - 1) / kPair2BN;
@@ -585,7 +598,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + kPair2Acc);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
+  const int nchunks = (nk + Cfg::CHUNK - 1) / Cfg::CHUNK;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -660,8 +673,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
           }
           tc::tc_fence_after();
           const uint32_t acc = tmem + uint32_t(b * kPair2BN);
-          const int kb1 = min(nk, (c + 1) * kTcChunk);
-          for (int kb = c * kTcChunk; kb < kb1; ++kb, ++it) {
+          const int kb1 = min(nk, (c + 1) * Cfg::CHUNK);
+          for (int kb = c * Cfg::CHUNK; kb < kb1; ++kb, ++it) {
             const int s = int(it % STAGES);
             if (!tc::mbar_wait(&full[s], (it / STAGES) & 1)) {
               atomicExch(err, kErrPairMma);
@@ -671,14 +684,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
             tc::tc_fence_after();
             const uint8_t* st = tiles_smem + s * Cfg::STAGE;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
+            for (int q = 0; q < Cfg::NPROD; ++q) {
               int pa, pb;
-              term_pair(q, pa, pb);
+              term_pair6(q, pa, pb);
               const uint64_t ad = tc::sdesc_kmajor_sw128(tc::smem_u32(st + pa * Cfg::A_TILE));
               const uint64_t bd = tc::sdesc_kmajor_sw128(tc::smem_u32(st + P * Cfg::A_TILE + pb * Cfg::B_TILE));
 #pragma unroll
               for (int j = 0; j < kTcBK / 16; ++j)
-                tc::mma_bf16_pair(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * kTcChunk) || q != 0 || j != 0);
+                tc::mma_bf16_pair(acc, ad + 2 * j, bd + 2 * j, idesc, (kb != c * Cfg::CHUNK) || q != 0 || j != 0);
             }
             tc::mma_commit_pair(&empty[s], 0x3);
           }
@@ -962,14 +975,16 @@ static gbblas_status_t launch_tc_pair(gbblas_handle_t h, const CUtensorMap& ta, 
   return after_launch("gemm_split_bf16_pair");
 }
 
-// 256 x 256 tiles on CTA pairs (x3, no split-K): a persistent grid of the
-// clusters that can be resident at once.
+// 256 x 256 tiles on CTA pairs (x3: three 64 KB stages; x6: two 96 KB
+// stages; no split-K): a persistent grid of the clusters that can be
+// resident at once.
+template <int P>
 static gbblas_status_t launch_tc_pair256(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb,
                                          int64_t M, int64_t N, int64_t nk, int64_t batch, float alpha, float beta,
                                          float* C, int64_t ldc, int64_t stride_c) {
-  constexpr int STAGES = 3;
-  using Cfg = Pair2Cfg<STAGES>;
-  auto* kern = gemm_split_bf16_pair256_kernel<STAGES>;
+  constexpr int STAGES = P == 2 ? 3 : 2;
+  using Cfg = Pair2Cfg<P, STAGES>;
+  auto* kern = gemm_split_bf16_pair256_kernel<P, STAGES>;
   static std::atomic<uint64_t> attr{0};
   GB_CUDA_TRY(raise_smem_limit(attr, reinterpret_cast<const void*>(kern), Cfg::SMEM, h->device));
   const int64_t tiles = cdiv(M, 2 * kTcBM) * cdiv(N, kPair2BN) * batch;
@@ -1031,9 +1046,9 @@ static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& 
     GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, kPairBHalf));
     return launch_tc_pair(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
   }
-  if (pair == 2 && P == 2 && split == 1) {
+  if (pair == 2 && split == 1) {
     GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, kPair2BHalf));
-    return launch_tc_pair256(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
+    return launch_tc_pair256<P>(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
   }
   GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, BN));
   if (split == 1)
@@ -1067,19 +1082,23 @@ static bool pair_tiles_enabled() {
   return on;
 }
 
-// The fixed split-BF16 modes: 256 x 128 CTA-pair tiles (x3) when there are
-// at least two waves of 128 x 128 tiles; 128 x 128 tiles when they fill the SMs; else
+// The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) when
+// every resident cluster gets at least eight; else 256 x 128 CTA-pair tiles
+// (x3) when there are at least two waves of 128 x 128 tiles; 128 x 128 tiles
+// when they fill the SMs; else
 // 128 x 64 tiles; and when even those leave half the SMs idle, split-K
 // slices of at least 4 k-blocks.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
   const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
+  const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
   if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) {
     // 256 x 256 cluster tiles when every resident cluster gets at least
     // eight, else 256 x 128
-    const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
     return split_gemm_run<128, 2>(h, g, 1, 0, t256 >= 8 * (sm / 2) ? 2 : 1);
   }
+  if (pieces == 3 && t256 >= 8 * (sm / 2) && g.k > 0 && pair_tiles_enabled())
+    return split_gemm_run<128, 3>(h, g, 1, 0, 2);
   if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 2);
   const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
   int64_t split = 1;

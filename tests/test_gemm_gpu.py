@@ -375,15 +375,17 @@ def test_gemm_strided_small_batch_tensor_cores(sb, torch_cuda, ta, tb, m, n, k, 
     sb.check_device_error()
 
 
+@pytest.mark.parametrize("mode", ["split_bf16x3", "split_bf16x6"])
 @pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
-def test_split_bf16x3_cta_pair_256_tiles(sb, torch_cuda, ta, tb):
-    """x3 on 256 x 256 CTA-pair tiles (taken when every resident cluster gets
-    at least eight): M and N not multiples of 256, K of two TMEM chunks and a
-    ragged last k-block, a strided batch, alpha and beta; against the oracle
-    at the x3 bound, and the rows and columns outside each C untouched."""
+def test_split_bf16_cta_pair_256_tiles(sb, torch_cuda, ta, tb, mode):
+    """x3 and x6 on 256 x 256 CTA-pair tiles (taken when every resident
+    cluster gets at least eight): M and N not multiples of 256, K of two or
+    three TMEM chunks and a ragged last k-block, a strided batch, alpha and
+    beta; against the oracle at the mode's bound, and the rows and columns
+    outside each C untouched."""
     torch = torch_cuda
     from portblas_gb300 import blas
-    sb.set_sgemm_mode(blas.sgemm_mode_t.split_bf16x3)
+    sb.set_sgemm_mode(getattr(blas.sgemm_mode_t, mode))
     m, n, k, batch = 1000, 1000, 300, 40  # 4 x 4 x 40 = 640 tiles of 256 x 256
     g = rng(m + n + k + int(ta) * 2 + int(tb) + 7)
     lda, ldb, ldc = (k if ta else m) + 3, (n if tb else k) + 5, m + 7
@@ -400,7 +402,7 @@ def test_split_bf16x3_cta_pair_256_tiles(sb, torch_cuda, ta, tb):
         scale = oracle.gemm_absscale(ta, tb, m, n, k, 0.75, a[i * sa:], lda, b[i * sbs:], ldb, 1.5, c[i * sc:],
                                      ldc)
         blk = out[i * sc:i * sc + ldc * n].reshape(n, ldc).T
-        assert (np.abs(blk[:m] - ref) / scale).max() <= norm_bound("split_bf16x3", k), i
+        assert (np.abs(blk[:m] - ref) / scale).max() <= norm_bound(mode, k), i
         np.testing.assert_array_equal(blk[m:], c[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:])
         np.testing.assert_array_equal(out[i * sc + ldc * n:(i + 1) * sc], c[i * sc + ldc * n:(i + 1) * sc])
     sb.check_device_error()
