@@ -567,7 +567,7 @@ struct Pair2Cfg {
   static constexpr int NPROD = P == 2 ? 3 : 6;
   // k-blocks per TMEM chunk: every product of the chunk goes into the one
   // accumulator, so x6 (six MMAs per K16 step) promotes twice as often
-  static constexpr int CHUNK = P == 2 ? kTcChunk : kTcChunk / 2;
+  static constexpr int CHUNK = P == 2 ? kTcChunk : kTcChunk / 4;
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
