@@ -64,8 +64,8 @@ gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g) {
   // AUTO: many small problems go to the one-CTA-per-problem kernel; shapes
   // beyond the largest the selector was trained on (2 m n k batch > 2^35
   // flop) that were not autotuned take the fixed x6 path (FP32-accurate,
-  // grouped-raster 128 x 128 tiles: 8192^3 at 274 TFLOP/s against 236 for
-  // the selector's extrapolated pick); otherwise every config is
+  // 256 x 256 CTA-pair tiles: 8192^3 at 322 TFLOP/s against 236 for the
+  // selector's extrapolated pick); otherwise every config is
   // FP32-accurate and the selector picks one
   if (small_batched_applies(g, h->sm_count)) return launch_gemm_small_batched(h, g);
   if (2.0 * double(g.m) * double(g.n) * double(g.k) * double(g.batch) > double(int64_t(1) << 35) &&
