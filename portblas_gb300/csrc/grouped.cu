@@ -58,6 +58,9 @@ struct GroupedProblem {
   int splits, kbs;
   int64_t part_off, tick_off;
   int64_t src;  // index of the problem in the caller's arrays
+  // tcgen05 tiles, BF16 in: bit 0 / bit 1 set when A / B is read in place
+  // with its rows contiguous (MN-major shared-memory tiles)
+  int mn;
 };
 
 constexpr int kGT = 64, kGK = 16, kGThreads = 256;
@@ -407,6 +410,7 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
     p.part_off = 0;
     p.tick_off = 0;
     p.src = i;
+    p.mn = 0;
     tab.push_back(p);
   }
   if (split_bk > 0) {
@@ -439,25 +443,38 @@ static gbblas_status_t build_table(int dtype, int64_t count, const char* transa,
   return GBBLAS_STATUS_SUCCESS;
 }
 
+// MN-major in-place tiles for BF16 operands whose rows are contiguous
+// (GBBLAS_GROUPED_MN=0 turns them off: such operands are then transposed by
+// the conversion pass).
+static bool mn_tiles_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("GBBLAS_GROUPED_MN");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 // One operand of the tcgen05 path: converted into BF16 terms (offset into
-// the term area) or, for a BF16 operand already K-contiguous with a 16-byte
-// aligned leading dimension, mapped in place.
+// the term area) or, for a BF16 operand with a 16-byte-aligned base and
+// leading dimension, mapped in place: K-contiguous (direct) or with its rows
+// contiguous (mn: the tile kernel loads 64-row boxes into MN-major tiles).
 struct TcOperandPlan {
   int prob, which;  // which: 0 = A (rows m), 1 = B (rows n)
-  bool direct;
+  bool direct, mn;
   int64_t rows, k, sr, Kp;
   const void* src;
   size_t off;
   int64_t sk;
 };
 
-static void plan_tc_operands(int dtype, const std::vector<GroupedProblem>& tab, std::vector<TcOperandPlan>& pl,
+static void plan_tc_operands(int dtype, std::vector<GroupedProblem>& tab, std::vector<TcOperandPlan>& pl,
                              size_t& term_bytes) {
   const int P = dtype == GBBLAS_DTYPE_BF16 ? 1 : 3;
   pl.clear();
   term_bytes = 0;
   for (size_t i = 0; i < tab.size(); ++i) {
-    const GroupedProblem& p = tab[i];
+    GroupedProblem& p = tab[i];
+    p.mn = 0;
     if (p.k == 0) continue;
     for (int which = 0; which < 2; ++which) {
       TcOperandPlan o{};
@@ -478,9 +495,11 @@ static void plan_tc_operands(int dtype, const std::vector<GroupedProblem>& tab, 
         o.src = p.b;
       }
       o.sk = sk;
-      o.direct = dtype == GBBLAS_DTYPE_BF16 && sk == 1 && o.sr % 8 == 0 && o.sr >= o.k &&
-                 (reinterpret_cast<uintptr_t>(o.src) & 15) == 0;
-      if (!o.direct) {
+      const bool al16 = (reinterpret_cast<uintptr_t>(o.src) & 15) == 0;
+      o.direct = dtype == GBBLAS_DTYPE_BF16 && sk == 1 && o.sr % 8 == 0 && o.sr >= o.k && al16;
+      o.mn = dtype == GBBLAS_DTYPE_BF16 && o.sr == 1 && sk % 8 == 0 && sk >= o.rows && al16 && mn_tiles_enabled();
+      if (o.mn) p.mn |= 1 << which;
+      if (!o.direct && !o.mn) {
         o.Kp = cdiv(o.k, int64_t(16)) * 16;
         o.off = term_bytes;
         term_bytes += (size_t(P) * size_t(o.rows) * size_t(o.Kp) * 2 + 255) & ~size_t(255);
@@ -508,7 +527,17 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
     cuuint64_t dims[3], strides[2];
     const int bk = dtype == GBBLAS_DTYPE_BF16 ? GtCfg<1>::BK : GtCfg<3>::BK;
     cuuint32_t box[3] = {cuuint32_t(bk), cuuint32_t(o.which == 0 ? kGtBM : kGtBN), 1};
-    if (o.direct) {
+    if (o.mn) {
+      // rows contiguous: boxes of 64 rows (128 bytes) x 64 k, two per tile
+      base = const_cast<void*>(o.src);
+      dims[0] = cuuint64_t(o.rows);
+      dims[1] = cuuint64_t(o.k);
+      dims[2] = 1;
+      strides[0] = cuuint64_t(o.sk) * 2;
+      strides[1] = cuuint64_t(o.sk) * 2 * cuuint64_t(o.k);
+      box[0] = cuuint32_t(kGtMnBox);
+      box[1] = cuuint32_t(bk);
+    } else if (o.direct) {
       base = const_cast<void*>(o.src);
       dims[0] = cuuint64_t(o.k);
       dims[1] = cuuint64_t(o.rows);
@@ -641,7 +670,7 @@ static gbblas_status_t prepare_host(gbblas_handle_t h, int dtype, int method, in
     H.maps.assign(2 * std::max<size_t>(1, H.tab.size()), CUtensorMap{});
     size_t n_conv = 0, n_ctas = 0;
     for (const TcOperandPlan& o : H.operands)
-      if (!o.direct) {
+      if (!o.direct && !o.mn) {
         ++n_conv;
         n_ctas += size_t(cdiv(gt_split_blocks(o.rows, o.Kp, o.sk == 1), int64_t(kGtSplitTiles)));
       }

@@ -341,6 +341,7 @@ __host__ __device__ inline int gt_fold_nodes(int splits) {
 // One scheduled tile (prob < 0: no more tiles).
 struct GtWork {
   int prob, nk, m0, n0;  // problem, k-blocks of this slice, tile origin
+  int mn;                // bit 0 / 1: A / B tiles are MN-major (rows contiguous, read in place)
   int m, n;              // the problem's C extent
   int kb0;               // first k-block of this slice
   int slice, splits;     // K slice of the output tile, and their number
@@ -353,6 +354,15 @@ struct GtWork {
 
 // tiles the scheduler takes from the counter at a time
 constexpr int kGtBatch = 8;
+
+// MN-major BF16 tiles (operands read in place with their rows contiguous):
+// two TMA boxes of kGtMnBox rows (128 bytes) x 64 k, kGtMnAtom bytes apart;
+// the descriptor's leading-dimension offset is the step between those
+// 64-row atoms along MN, its stride offset the step between 8-row groups
+// along K (checked against the oracle: the swapped assignment gives wrong
+// products, not a fault, since both stay inside the stage)
+constexpr int kGtMnBox = 64, kGtMnAtom = kGtMnBox * kGtBK * 2;
+constexpr uint32_t kGtMnLbo = kGtMnAtom, kGtMnSbo = 1024;
 
 enum : int { kErrGtProducer = 401, kErrGtMma = 402, kErrGtEpilogue = 403, kErrGtDrain = 404 };
 
@@ -437,6 +447,7 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           const int tiles_m = (pr.m + kGtBM - 1) / kGtBM;
           const int nk_all = pr.k > 0 ? (pr.k + Cfg::BK - 1) / Cfg::BK : 0;
           w.prob = p;
+          w.mn = pr.mn;
           w.splits = pr.splits;
           w.slice = 0;
           w.kb0 = 0;
@@ -523,8 +534,19 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           }
           tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
           uint8_t* st = smem + s * Cfg::STAGE;
-          tc::tma_load_3d(st, ma, &full[s], (w.kb0 + kb) * Cfg::BK, w.m0, 0);
-          tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], (w.kb0 + kb) * Cfg::BK, w.n0, 0);
+          const int kc = (w.kb0 + kb) * Cfg::BK;
+          if (P == 1 && (w.mn & 1)) {  // two boxes of 64 rows: MN-major tile
+            tc::tma_load_3d(st, ma, &full[s], w.m0, kc, 0);
+            tc::tma_load_3d(st + kGtMnAtom, ma, &full[s], w.m0 + kGtMnBox, kc, 0);
+          } else {
+            tc::tma_load_3d(st, ma, &full[s], kc, w.m0, 0);
+          }
+          if (P == 1 && (w.mn & 2)) {
+            tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], w.n0, kc, 0);
+            tc::tma_load_3d(st + P * Cfg::A_TILE + kGtMnAtom, mb, &full[s], w.n0 + kGtMnBox, kc, 0);
+          } else {
+            tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kc, w.n0, 0);
+          }
         }
         if (!ok) break;
       }
@@ -574,7 +596,19 @@ __global__ void __launch_bounds__(kGtThreads, 1)
             auto desc = [](uint32_t a) {
               return Cfg::BK == 64 ? tc::sdesc_kmajor_sw128(a) : tc::sdesc_kmajor_sw64(a);
             };
-            if constexpr (P <= 2) {
+            if constexpr (P == 1) {
+              // K = 16 per MMA: +32 bytes in a K-major swizzled row, +2 8-row
+              // groups (2048 bytes) in an MN-major tile
+              const uint32_t sa = tc::smem_u32(st), sb = tc::smem_u32(st + Cfg::A_TILE);
+              const bool amn = w.mn & 1, bmn = w.mn & 2;
+              const uint64_t ad = amn ? tc::sdesc_mn_sw128<kGtMnLbo, kGtMnSbo>(sa) : desc(sa);
+              const uint64_t bd = bmn ? tc::sdesc_mn_sw128<kGtMnLbo, kGtMnSbo>(sb) : desc(sb);
+              const uint64_t astep = amn ? (2048 >> 4) : 2, bstep = bmn ? (2048 >> 4) : 2;
+              const uint32_t id = idesc | (amn ? 1u << 15 : 0u) | (bmn ? 1u << 16 : 0u);
+#pragma unroll
+              for (int j = 0; j < Cfg::BK / 16; ++j)
+                tc::mma_bf16(acc, ad + astep * j, bd + bstep * j, id, kb != c * CHUNK || j != 0);
+            } else if constexpr (P == 2) {
 #pragma unroll
               for (int q = 0; q < Cfg::NPAIRS; ++q) {  // (0,0) (0,1) (1,0)
                 const int pa = q == 2 ? 1 : 0, pb = q == 1 ? 1 : 0;

@@ -173,6 +173,24 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
   return d;
 }
 
+// Shared-memory matrix descriptor for an MN-major operand tile (rows of the
+// MMA operand contiguous) in the 128-byte-swizzled layout TMA produces from
+// boxes of 64 BF16 rows x k: each box is k rows of 128 B (64 MN elements),
+// 8-row groups 1024 B apart along K (SBO), boxes LBO bytes apart along MN.
+// Bits: [0,14) start >> 4, [16,30) leading-dim byte offset >> 4 (MN-major:
+// between 64-element atoms along MN), [32,46) stride byte offset >> 4
+// (between 8-row groups along K), [46,48) version 1, [61,64) SWIZZLE_128B.
+template <uint32_t LBO, uint32_t SBO>
+__device__ __forceinline__ uint64_t sdesc_mn_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr & 0x3FFFFu) >> 4);
+  d |= uint64_t(LBO >> 4) << 16;
+  d |= uint64_t(SBO >> 4) << 32;
+  d |= uint64_t(1) << 46;
+  d |= uint64_t(2) << 61;
+  return d;
+}
+
 // The same for the 64-byte swizzle (rows of 64 B, 8-row groups 512 B
 // apart): [32,46) stride byte offset 512 B, [61,64) layout 4 = SWIZZLE_64B.
 __device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {

@@ -227,6 +227,48 @@ def test_grouped_split_k_long_k(sb, torch_cuda, dtype, method):
 
 
 @pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
+@pytest.mark.parametrize("ta,tb", [(False, True), (False, False), (True, True)])
+def test_grouped_bf16_rows_contiguous_read_in_place(sb, torch_cuda, method, ta, tb):
+    """BF16 operands whose rows are contiguous (A 'n', B 't') with a leading
+    dimension that is a multiple of 8 elements and a 16-byte-aligned start
+    are read in place as MN-major tiles (two 64-row boxes per tile): rows
+    below, at and above 64 and 128 (second box partly or wholly outside),
+    ragged K, views 8 elements (16 bytes) and 1 element into a buffer (the
+    latter takes the conversion pass), a long-K problem cut into slices;
+    every C entry against the oracle."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(700 + 2 * ta + tb)
+    shapes = [(1, 1, 1), (8, 16, 5), (48, 48, 300), (64, 64, 64), (65, 130, 129), (128, 128, 200), (136, 72, 17),
+              (200, 256, 70), (40, 24, 20000)]
+    probs, host, keep = [], [], []
+    for i, (m, n, k) in enumerate(shapes):
+        shift = 8 if i % 3 == 1 else (1 if i % 3 == 2 and i < 8 else 0)
+        lda = k + 1 if ta else ((m + 7) // 8) * 8 + 8 * (i % 2)
+        ldb = ((n + 7) // 8) * 8 + 8 * ((i + 1) % 2) if tb else k + 3
+        ldc = m + 2
+        sa, sbs = lda * (m if ta else k), ldb * (k if tb else n)
+        a = torch.from_numpy(g.uniform(-1, 1, sa).astype(np.float32)).bfloat16()
+        b = torch.from_numpy(g.uniform(-1, 1, sbs).astype(np.float32)).bfloat16()
+        abuf = torch.zeros(shift + sa, dtype=torch.bfloat16, device="cuda")
+        bbuf = torch.zeros(shift + sbs, dtype=torch.bfloat16, device="cuda")
+        abuf[shift:].copy_(a.cuda())
+        bbuf[shift:].copy_(b.cuda())
+        keep += [abuf, bbuf]
+        c = g.uniform(-1, 1, ldc * n).astype(np.float32)
+        probs.append(dict(transa="t" if ta else "n", transb="t" if tb else "n", m=m, n=n, k=k, alpha=1.25,
+                          a=abuf[shift:], lda=lda, b=bbuf[shift:], ldb=ldb, beta=0.5,
+                          c=torch.from_numpy(c).cuda(), ldc=ldc))
+        host.append((ta, tb, m, n, k, 1.25, a.float().numpy(), lda, b.float().numpy(), ldb, 0.5, c, ldc))
+    plan = blas.GroupedPlan(sb, probs, dtype="bfloat16")
+    plan.run()
+    sb.wait()
+    _check(probs, host)
+    plan.close()
+    sb.check_device_error()
+
+
+@pytest.mark.parametrize("method", ["tcgen05"], indirect=True)
 @pytest.mark.parametrize("shift", [0, 1])
 def test_grouped_bf16_operand_alignment(sb, torch_cuda, method, shift):
     """BF16 operands moved into the K-major tiles with 32-bit loads: views
