@@ -458,9 +458,12 @@ static bool mn_tiles_enabled() {
 // the term area) or, for a BF16 operand with a 16-byte-aligned base and
 // leading dimension, mapped in place: K-contiguous (direct) or with its rows
 // contiguous (mn: the tile kernel loads 64-row boxes into MN-major tiles).
+// A BF16 operand with contiguous rows that TMA cannot address in place is
+// copied (not transposed) by the pass into a 16-byte pitch and read as
+// MN-major tiles from there (mn and !direct, Kp: the row pitch).
 struct TcOperandPlan {
   int prob, which;  // which: 0 = A (rows m), 1 = B (rows n)
-  bool direct, mn;
+  bool direct, mn, copy;
   int64_t rows, k, sr, Kp;
   const void* src;
   size_t off;
@@ -497,9 +500,15 @@ static void plan_tc_operands(int dtype, std::vector<GroupedProblem>& tab, std::v
       o.sk = sk;
       const bool al16 = (reinterpret_cast<uintptr_t>(o.src) & 15) == 0;
       o.direct = dtype == GBBLAS_DTYPE_BF16 && sk == 1 && o.sr % 8 == 0 && o.sr >= o.k && al16;
-      o.mn = dtype == GBBLAS_DTYPE_BF16 && o.sr == 1 && sk % 8 == 0 && sk >= o.rows && al16 && mn_tiles_enabled();
-      if (o.mn) p.mn |= 1 << which;
-      if (!o.direct && !o.mn) {
+      const bool rows_contig = dtype == GBBLAS_DTYPE_BF16 && o.sr == 1 && sk != 1 && mn_tiles_enabled();
+      o.mn = rows_contig && sk % 8 == 0 && sk >= o.rows && al16;
+      o.copy = rows_contig && !o.mn;
+      if (o.mn || o.copy) p.mn |= 1 << which;
+      if (o.copy) {
+        o.Kp = cdiv(o.rows, int64_t(16)) * 16;  // row pitch of the copy
+        o.off = term_bytes;
+        term_bytes += (size_t(o.Kp) * size_t(o.k) * 2 + 255) & ~size_t(255);
+      } else if (!o.direct && !o.mn) {
         o.Kp = cdiv(o.k, int64_t(16)) * 16;
         o.off = term_bytes;
         term_bytes += (size_t(P) * size_t(o.rows) * size_t(o.Kp) * 2 + 255) & ~size_t(255);
@@ -527,16 +536,33 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
     cuuint64_t dims[3], strides[2];
     const int bk = dtype == GBBLAS_DTYPE_BF16 ? GtCfg<1>::BK : GtCfg<3>::BK;
     cuuint32_t box[3] = {cuuint32_t(bk), cuuint32_t(o.which == 0 ? kGtBM : kGtBN), 1};
-    if (o.mn) {
-      // rows contiguous: boxes of 64 rows (128 bytes) x 64 k, two per tile
-      base = const_cast<void*>(o.src);
+    if (o.mn || o.copy) {
+      // rows contiguous: boxes of 64 rows (128 bytes) x 64 k, two per tile,
+      // in place or from the pass's copy
+      const int64_t pitch = o.copy ? o.Kp : o.sk;
+      base = o.copy ? static_cast<void*>(terms + o.off) : const_cast<void*>(o.src);
       dims[0] = cuuint64_t(o.rows);
       dims[1] = cuuint64_t(o.k);
       dims[2] = 1;
-      strides[0] = cuuint64_t(o.sk) * 2;
-      strides[1] = cuuint64_t(o.sk) * 2 * cuuint64_t(o.k);
+      strides[0] = cuuint64_t(pitch) * 2;
+      strides[1] = cuuint64_t(pitch) * 2 * cuuint64_t(o.k);
       box[0] = cuuint32_t(kGtMnBox);
       box[1] = cuuint32_t(bk);
+      if (o.copy) {
+        // the copy is the pass's K-contiguous case with rows and K swapped:
+        // line k (stride sk in the source) of `rows` contiguous elements
+        GtOperand g;
+        g.src = o.src;
+        g.sr = o.sk;
+        g.sk = 1;
+        g.rows = int(o.k);
+        g.K = int(o.rows);
+        g.Kp = int(o.Kp);
+        g.blocks = int(gt_split_blocks(o.k, o.Kp, true, true));
+        g.parts = int(cdiv(int64_t(g.blocks), int64_t(kGtSplitTiles)));
+        g.out = reinterpret_cast<__nv_bfloat16*>(terms + o.off);
+        ops.push_back(g);
+      }
     } else if (o.direct) {
       base = const_cast<void*>(o.src);
       dims[0] = cuuint64_t(o.k);
@@ -559,7 +585,7 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
       g.rows = int(o.rows);
       g.K = int(o.k);
       g.Kp = int(o.Kp);
-      g.blocks = int(gt_split_blocks(o.rows, o.Kp, g.sk == 1));
+      g.blocks = int(gt_split_blocks(o.rows, o.Kp, g.sk == 1, P == 1));
       g.parts = int(cdiv(int64_t(g.blocks), int64_t(kGtSplitTiles)));
       g.out = reinterpret_cast<__nv_bfloat16*>(terms + o.off);
       ops.push_back(g);
@@ -670,9 +696,12 @@ static gbblas_status_t prepare_host(gbblas_handle_t h, int dtype, int method, in
     H.maps.assign(2 * std::max<size_t>(1, H.tab.size()), CUtensorMap{});
     size_t n_conv = 0, n_ctas = 0;
     for (const TcOperandPlan& o : H.operands)
-      if (!o.direct && !o.mn) {
+      if (o.copy) {
         ++n_conv;
-        n_ctas += size_t(cdiv(gt_split_blocks(o.rows, o.Kp, o.sk == 1), int64_t(kGtSplitTiles)));
+        n_ctas += size_t(cdiv(gt_split_blocks(o.k, o.Kp, true, true), int64_t(kGtSplitTiles)));
+      } else if (!o.direct && !o.mn) {
+        ++n_conv;
+        n_ctas += size_t(cdiv(gt_split_blocks(o.rows, o.Kp, o.sk == 1, bf16), int64_t(kGtSplitTiles)));
       }
     H.ops.resize(n_conv);
     H.ctas.resize(n_ctas);

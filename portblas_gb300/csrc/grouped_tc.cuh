@@ -98,11 +98,15 @@ struct GtOperand {
 // ceil(b / kGtSplitTiles) CTAs, so every CTA has about the same work)
 constexpr int kGtSplitTiles = 2;
 
-// Tiles of an operand's conversion: K-contiguous operands (sk == 1) in
-// 32-row x 128-k tiles with no transpose, the others in 64 x 64 tiles
-// transposed through shared memory.
-__host__ __device__ inline int64_t gt_split_blocks(int64_t rows, int64_t Kp, bool kcontig) {
-  return kcontig ? ((rows + 31) / 32) * ((Kp + 127) / 128) : ((rows + 63) / 64) * ((Kp + 63) / 64);
+// Tiles of an operand's conversion: K-contiguous operands (sk == 1) with no
+// transpose, BF16 ones (flat) in blocks of kGtFlat consecutive elements of
+// the rows x Kp output (short rows share a block), FP32 ones (three terms)
+// in 32-row x 128-k tiles; the others in 64 x 64 tiles transposed through
+// shared memory.
+constexpr int kGtFlat = 4096;
+__host__ __device__ inline int64_t gt_split_blocks(int64_t rows, int64_t Kp, bool kcontig, bool flat) {
+  if (!kcontig) return ((rows + 63) / 64) * ((Kp + 63) / 64);
+  return flat ? (rows * Kp + kGtFlat - 1) / kGtFlat : ((rows + 31) / 32) * ((Kp + 127) / 128);
 }
 
 template <typename T>
@@ -188,25 +192,50 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
   __nv_bfloat16* __restrict__ out = op.out;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int64_t plane = int64_t(op.rows) * op.Kp;
+  if constexpr (sizeof(T) == 2) {
+    if (op.sk == 1) {
+      // K-contiguous BF16 (its own single term: the raw 16-bit values move):
+      // block j is elements [j * kGtFlat, +kGtFlat) of the rows x Kp output,
+      // row after row; lane l of warp w moves the four elements from
+      // w * kGtFlat / 8 + 128 i + 4 l (i < 4): rows shorter than 128 pack into
+      // one warp step instead of leaving lanes idle (Kp is a multiple of 16,
+      // so a 4-element group never crosses a row)
+      const int64_t total = int64_t(op.rows) * op.Kp;
+      const int rq = 128 / op.Kp, rk = 128 % op.Kp;  // a 128-element step in rows and columns
+      const __nv_bfloat16* Xh = reinterpret_cast<const __nv_bfloat16*>(X);
+      for (int j = part; j < op.blocks; j += op.parts) {
+        const int64_t e0 = int64_t(j) * kGtFlat + warp * (kGtFlat / 8) + 4 * lane;
+        if (e0 >= total) continue;
+        int64_t rr[4];
+        int kk[4];
+        rr[0] = e0 / op.Kp;
+        kk[0] = int(e0 - rr[0] * op.Kp);
+#pragma unroll
+        for (int i = 1; i < 4; ++i) {
+          kk[i] = kk[i - 1] + rk;
+          rr[i] = rr[i - 1] + rq;
+          if (kk[i] >= op.Kp) {
+            kk[i] -= op.Kp;
+            ++rr[i];
+          }
+        }
+        uint2 q[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          q[i] = rr[i] < op.rows ? gt_ld4_raw(Xh + rr[i] * op.sr + kk[i], kk[i], op.K) : make_uint2(0u, 0u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (rr[i] < op.rows) *reinterpret_cast<uint2*>(out + rr[i] * op.Kp + kk[i]) = q[i];
+      }
+      return;
+    }
+  }
   if (op.sk == 1) {
-    // K-contiguous: warp w converts rows 4w .. 4w+3 of the tile, lane l the
-    // four k from 4l (and from 4l + 128 ... in later tiles)
+    // K-contiguous FP32: warp w converts rows 4w .. 4w+3 of a 32 x 128 tile,
+    // lane l the four k from 4l
     const int nkb = (op.Kp + 127) / 128;
     for (int j = part; j < op.blocks; j += op.parts) {
       const int64_t r0 = int64_t(j / nkb) * 32 + warp * 4, k = int64_t(j % nkb) * 128 + 4 * lane;
-      if constexpr (sizeof(T) == 2) {
-        // BF16 is its own single term: move the raw 16-bit values
-        uint2 q[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) q[i] = (r0 + i < op.rows) ? gt_ld4_raw(X + (r0 + i) * op.sr + k, k, op.K)
-                                                              : make_uint2(0u, 0u);
-        if (k < op.Kp) {
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (r0 + i < op.rows) *reinterpret_cast<uint2*>(out + (r0 + i) * op.Kp + k) = q[i];
-        }
-        continue;
-      }
       float v[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
