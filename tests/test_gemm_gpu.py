@@ -379,7 +379,7 @@ def test_gemm_strided_small_batch_tensor_cores(sb, torch_cuda, ta, tb, m, n, k, 
 @pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
 def test_split_bf16_cta_pair_256_tiles(sb, torch_cuda, ta, tb, mode):
     """x3 and x6 on 256 x 256 CTA-pair tiles (taken when every resident
-    cluster gets at least eight): M and N not multiples of 256, K of two or
+    cluster gets at least two): M and N not multiples of 256, K of two or
     three TMEM chunks and a ragged last k-block, a strided batch, alpha and
     beta; against the oracle at the mode's bound, and the rows and columns
     outside each C untouched."""
