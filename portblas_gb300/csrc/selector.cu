@@ -220,20 +220,36 @@ static std::string shape_key(const GemmArgs<T>& g) {
   return buf;
 }
 
+// the network's picks, per shape key (every input of the network is part of
+// the key, so a remembered pick is the one the network would make again);
+// cleared when it grows past kPickCacheMax entries
+static std::unordered_map<std::string, int>& picked() {
+  static std::unordered_map<std::string, int> t;
+  return t;
+}
+constexpr size_t kPickCacheMax = 4096;
+
 template <typename T>
 static int select_config(const GemmArgs<T>& g) {
   const int dtype = sizeof(T) == 8 ? kSelF64 : kSelF32;
+  const std::string key = shape_key(g);
   {
     std::lock_guard<std::mutex> lk(g_tuned_mu);
-    auto it = tuned().find(shape_key(g));
+    auto it = tuned().find(key);
     if (it != tuned().end()) return it->second;
+    auto ip = picked().find(key);
+    if (ip != picked().end()) return ip->second;
   }
   load_default_selector();
   const MlpSelector& s = selector();
   if (s.loaded) {
     float f[kSgemmFeatures];
     gemm_features(g.m, g.n, g.k, g.ta, g.tb, g.lda, g.ldb, g.ldc, g.batch, dtype, f);
-    return dtype == kSelF64 ? mlp_pick(s, f, kDgemmFirst, kGemmConfigs) : mlp_pick(s, f, 0, kSgemmConfigs);
+    const int c = dtype == kSelF64 ? mlp_pick(s, f, kDgemmFirst, kGemmConfigs) : mlp_pick(s, f, 0, kSgemmConfigs);
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
+    if (picked().size() >= kPickCacheMax) picked().clear();
+    picked()[key] = c;
+    return c;
   }
   return heuristic_config(g.m, g.n, g.batch, dtype);
 }
@@ -371,7 +387,9 @@ gbblas_status_t gbblas_sgemm_load_selector(const char* path) {
   clear_error();
   MlpSelector s;
   if (!path || !load_selector_file(path, s)) return fail(GBBLAS_STATUS_INVALID_ARG, "selector: cannot load weights");
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
   selector() = s;
+  picked().clear();  // the new weights pick afresh
   return GBBLAS_STATUS_SUCCESS;
 }
 

@@ -102,3 +102,32 @@ def test_selector_weight_file_format(tmp_path, L):
     shipped = __import__("os").path.join(__import__("os").path.dirname(build.LIB_PATH), "..", "tuning",
                                          "gemm_selector.bin")
     assert L.gbblas_sgemm_load_selector(shipped.encode()) == 0
+
+
+def test_selector_picks_are_remembered_and_reset_by_new_weights(tmp_path, L):
+    """AUTO remembers the network's pick per shape; loading new weights
+    forgets it.  Two weight files whose output layer makes config 7, then
+    config 23, the fastest for every input: the same shape picks 7, then 23."""
+    from portblas_gb300.tuning import train
+    cfg = C.c_int()
+    paths = []
+    for winner in (7, 23):
+        p = train.init_params(5)
+        out = train.OUT
+        p[-(out * train.HID + out):] = 0.0  # last layer: weights and biases
+        p[-out + winner] = -100.0           # predicted log-time: lowest wins
+        path = tmp_path / f"w{winner}.bin"
+        train.write_bin(str(path), p)
+        paths.append(path)
+    try:
+        assert L.gbblas_sgemm_load_selector(str(paths[0]).encode()) == 0
+        for _ in range(2):
+            assert L.gbblas_sgemm_selector_pick(700, 300, 900, b"n", b"t", 704, 304, 700, 1, C.byref(cfg)) == 0
+            assert cfg.value == 7
+        assert L.gbblas_sgemm_load_selector(str(paths[1]).encode()) == 0
+        assert L.gbblas_sgemm_selector_pick(700, 300, 900, b"n", b"t", 704, 304, 700, 1, C.byref(cfg)) == 0
+        assert cfg.value == 23
+    finally:
+        shipped = __import__("os").path.join(__import__("os").path.dirname(build.LIB_PATH), "..", "tuning",
+                                             "gemm_selector.bin")
+        assert L.gbblas_sgemm_load_selector(shipped.encode()) == 0
