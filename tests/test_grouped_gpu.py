@@ -369,3 +369,22 @@ def test_grouped_no_split_for_many_short_problems(sb, torch_cuda, method):
     plan = blas.GroupedPlan(sb, probs, dtype="float32")
     assert plan.info()[1] == 1
     plan.close()
+
+
+def test_grouped_bf16_transposing_pass_when_mn_tiles_off():
+    """With GBBLAS_GROUPED_MN=0 (read once per process, so in a child
+    pytest) BF16 operands whose rows are contiguous go through the
+    conversion pass's transposing path into K-major tiles: the alignment and
+    rows-contiguous cases against the oracle there."""
+    import os
+    import subprocess
+    import sys
+    if os.environ.get("GBBLAS_GROUPED_MN") == "0":
+        pytest.skip("already the child run")
+    env = dict(os.environ, GBBLAS_GROUPED_MN="0")
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider",
+                        os.path.join(here, "test_grouped_gpu.py"), "-k",
+                        "bf16_operand_alignment or rows_contiguous or bf16_aligned_operands"],
+                       env=env, cwd=os.path.dirname(here), capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
