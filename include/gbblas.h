@@ -197,8 +197,8 @@ gbblas_status_t gbblas_dgemv(gbblas_handle_t h, char trans, int64_t m, int64_t n
  * problem needing more scratch is rejected with GBBLAS_STATUS_INVALID_ARG
  * before any kernel runs.  Each call enqueues one cudaMemsetAsync clearing
  * 4 bytes of tickets per output element (at most 256 KiB).  The first call on
- * a device looks the block up (cudaGetSymbolAddress): make it before any
- * stream capture.  All calls share the block, so calls that overlap on the
+ * a device looks the block's address up (cudaGetSymbolAddress, a synchronous
+ * runtime call).  All calls share the block, so calls that overlap on the
  * GPU race.  A device-side wait that gives up (2 s) is not reported by this
  * call (it has returned SUCCESS; y may be wrong): use gbblas_sgemv with a
  * handle and gbblas_check_device_error where that must be seen. */

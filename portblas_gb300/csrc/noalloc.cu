@@ -19,8 +19,8 @@
 //   * every GPU that loads the library holds the arrays (1 MiB + 256 KiB)
 //     until the process exits;
 //   * the first call on each device looks up the arrays' device addresses
-//     (cudaGetSymbolAddress with that device current) — make that first
-//     call before any stream capture;
+//     (cudaGetSymbolAddress with that device current, a synchronous runtime
+//     call);
 //   * the stream must belong to the current device (INVALID_ARG otherwise);
 //   * all calls share the arrays: calls that overlap on the GPU (different
 //     streams, no ordering between them) race and give wrong results;
