@@ -550,7 +550,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
 // one accumulator (two of 256 columns, so the MMAs of the next chunk run
 // while the epilogue promotes this one); sixteen epilogue warps per CTA, four
 // per TMEM lane quarter, each with 64 of the 256 columns.  Used where the
-// 256 x 256 tiles give every resident cluster at least two rounds.
+// 256 x 256 tiles fill at least half of the resident clusters.
 constexpr int kPair2BN = 256, kPair2BHalf = kPair2BN / 2;
 constexpr int kPair2EpiWarps = 16, kPair2Threads = 32 * (2 + kPair2EpiWarps);
 constexpr int kPair2Acc = 2;
@@ -1082,24 +1082,23 @@ static bool pair_tiles_enabled() {
   return on;
 }
 
-// The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) when
-// every resident cluster gets at least two; else 256 x 128 CTA-pair tiles
-// (x3) when there are at least two waves of 128 x 128 tiles; 128 x 128 tiles
-// when they fill the SMs; else
+// The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) when M
+// and N are at least 256 and the tiles fill at least half of the resident
+// clusters (x3 / x6 TFLOP/s against the next choice: 2048^3 267 / 185 against
+// 225 / 170, 3072^3 430 / 250 against 358 / 208, 6144^3 572 / 308 against
+// 452 / 252; the uneven last round costs less than the smaller tiles'
+// lower MMA rate); else 256 x 128 CTA-pair tiles (x3) when there are at
+// least two waves of 128 x 128 tiles; 128 x 128 tiles when they fill the
+// SMs; else
 // 128 x 64 tiles; and when even those leave half the SMs idle, split-K
 // slices of at least 4 k-blocks.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
   const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
   const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
-  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) {
-    // 256 x 256 cluster tiles when every resident cluster gets at least
-    // two (4096^3 - 6144^3: 13-27% faster than 256 x 128 despite the uneven
-    // last round), else 256 x 128
-    return split_gemm_run<128, 2>(h, g, 1, 0, t256 >= 2 * (sm / 2) ? 2 : 1);
-  }
-  if (pieces == 3 && t256 >= 2 * (sm / 2) && g.k > 0 && pair_tiles_enabled())
-    return split_gemm_run<128, 3>(h, g, 1, 0, 2);
+  if (g.k > 0 && pair_tiles_enabled() && 2 * t256 >= (sm / 2) && g.m >= 2 * kTcBM && g.n >= kPair2BN)
+    return pieces == 2 ? split_gemm_run<128, 2>(h, g, 1, 0, 2) : split_gemm_run<128, 3>(h, g, 1, 0, 2);
+  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) return split_gemm_run<128, 2>(h, g, 1, 0, 1);
   if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 2);
   const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
   int64_t split = 1;

@@ -378,8 +378,9 @@ def test_gemm_strided_small_batch_tensor_cores(sb, torch_cuda, ta, tb, m, n, k, 
 @pytest.mark.parametrize("mode", ["split_bf16x3", "split_bf16x6"])
 @pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
 def test_split_bf16_cta_pair_256_tiles(sb, torch_cuda, ta, tb, mode):
-    """x3 and x6 on 256 x 256 CTA-pair tiles (taken when every resident
-    cluster gets at least two): M and N not multiples of 256, K of two or
+    """x3 and x6 on 256 x 256 CTA-pair tiles (taken when M and N are at
+    least 256 and the tiles fill half of the resident clusters): M and N not
+    multiples of 256, K of two or
     three TMEM chunks and a ragged last k-block, a strided batch, alpha and
     beta; against the oracle at the mode's bound, and the rows and columns
     outside each C untouched."""
@@ -410,14 +411,15 @@ def test_split_bf16_cta_pair_256_tiles(sb, torch_cuda, ta, tb, mode):
 
 @pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
 def test_split_bf16x3_cta_pair_tiles(sb, torch_cuda, ta, tb):
-    """x3 on 256 x 128 CTA-pair tiles (taken when there are at least two
-    waves of 128 x 128 tiles): M not a multiple of 256, ragged N and K, a
-    strided batch, alpha and beta; against the oracle at the x3 bound, and
-    the rows and columns outside each C untouched."""
+    """x3 on 256 x 128 CTA-pair tiles (taken when N is below 256, which
+    rules out 256 x 256 tiles, and there are at least two waves of 128 x 128
+    tiles): M not a multiple of 256, ragged N and K, a strided batch, alpha
+    and beta; against the oracle at the x3 bound, and the rows and columns
+    outside each C untouched."""
     torch = torch_cuda
     from portblas_gb300 import blas
     sb.set_sgemm_mode(blas.sgemm_mode_t.split_bf16x3)
-    m, n, k, batch = 1000, 600, 300, 8  # 8 x 5 x 8 = 320 tiles of 128 x 128
+    m, n, k, batch = 1000, 200, 300, 20  # 8 x 2 x 20 = 320 tiles of 128 x 128
     g = rng(m + n + k + int(ta) * 2 + int(tb))
     lda, ldb, ldc = (k if ta else m) + 3, (n if tb else k) + 5, m + 7
     sa, sbs, sc = lda * (m if ta else k), ldb * (k if tb else n), ldc * n + 11
