@@ -62,13 +62,17 @@ gbblas_status_t dispatch_gemm(gbblas_handle_t h, const GemmArgs<float>& g) {
     default: break;
   }
   // AUTO: many small problems go to the one-CTA-per-problem kernel; shapes
-  // beyond the largest the selector was trained on (2 m n k batch > 2^35
-  // flop) that were not autotuned take the fixed x6 path (FP32-accurate,
-  // 256 x 256 CTA-pair tiles: 8192^3 at 322 TFLOP/s against 236 for the
-  // selector's extrapolated pick); otherwise every config is
-  // FP32-accurate and the selector picks one
+  // that were not autotuned take the fixed x6 path (FP32-accurate) when they
+  // are beyond the largest the selector was trained on (2 m n k batch > 2^35
+  // flop: 8192^3 at 322 TFLOP/s against 236 for the selector's extrapolated
+  // pick) or when they fit the 256 x 256 CTA-pair tiles, which the
+  // selector's configs do not include (against its picks: 2048^3 219 / 185,
+  // 4096^2 x 512 208 / 153, 8192^2 x 128 174 / 70, 1792^2 x 4096 185 / 153
+  // TFLOP/s); otherwise every config is FP32-accurate and the selector
+  // picks one
   if (small_batched_applies(g, h->sm_count)) return launch_gemm_small_batched(h, g);
-  if (2.0 * double(g.m) * double(g.n) * double(g.k) * double(g.batch) > double(int64_t(1) << 35) &&
+  if ((2.0 * double(g.m) * double(g.n) * double(g.k) * double(g.batch) > double(int64_t(1) << 35) ||
+       split_bf16_pair256_fits(g, h->sm_count)) &&
       !has_tuned_config(g))
     return launch_gemm_split_bf16(h, g, 3);
   gbblas_status_t s = launch_sgemm_config(h, g, select_sgemm_config(h, g));

@@ -49,6 +49,9 @@ gbblas_status_t launch_scale_c(gbblas_handle_t h, int64_t m, int64_t n, double b
 // Split-BF16 FP32 GEMM on the tcgen05 tensor cores (pieces = 2 or 3 BF16
 // terms per operand).  Returns UNSUPPORTED when the shape is not handled.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces);
+// The fixed split-BF16 modes take 256 x 256 CTA-pair tiles for this shape
+// (M and N at least 256, enough tiles, the last round filled well enough).
+bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm_count);
 // Same with an explicit N tile (64 or 128), split-K factor and raster order
 // (raster_m: consecutive CTAs walk down M).
 gbblas_status_t launch_gemm_split_bf16_cfg(gbblas_handle_t h, const GemmArgs<float>& g, int pieces, int bn,

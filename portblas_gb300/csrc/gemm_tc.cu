@@ -1082,21 +1082,34 @@ static bool pair_tiles_enabled() {
   return on;
 }
 
-// The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) when M
-// and N are at least 256 and the tiles fill at least half of the resident
-// clusters (x3 / x6 TFLOP/s against the next choice: 2048^3 267 / 185 against
-// 225 / 170, 3072^3 430 / 250 against 358 / 208, 6144^3 572 / 308 against
-// 452 / 252; the uneven last round costs less than the smaller tiles'
-// lower MMA rate); else 256 x 128 CTA-pair tiles (x3) when there are at
-// least two waves of 128 x 128 tiles; 128 x 128 tiles when they fill the
+// 256 x 256 CTA-pair tiles: M and N at least 256, tiles for at least half
+// of the resident clusters, and their rounds filled at least 0.8 x as well
+// as those of 128 x 128 one-CTA tiles (the pair tile's MMA rate per SM is
+// about 1.3 x higher).  x3 / x6 TFLOP/s against the next choice: 2048^3 267 /
+// 185 against 225 / 170, 3072^3 430 / 250 against 358 / 208, 6144^3 572 /
+// 308 against 452 / 252; 2304^3 (81 tiles: a second round of 5) and 2560^3
+// (100) ran 2-4% slower on the pair tiles, and the fill rule leaves them out.
+bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm) {
+  if (g.k <= 0 || g.m < 2 * kTcBM || g.n < kPair2BN || !pair_tiles_enabled()) return false;
+  const int64_t clusters = sm / 2;
+  const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
+  const int64_t t128 = cdiv(g.m, kTcBM) * cdiv(g.n, 128) * g.batch;
+  if (clusters < 1 || 2 * t256 < clusters) return false;
+  const double fill256 = double(t256) / double(cdiv(t256, clusters) * clusters);
+  const double fill128 = double(t128) / double(cdiv(t128, sm) * sm);
+  return fill256 >= 0.8 * fill128;
+}
+
+// The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) where
+// split_bf16_pair256_fits; else 256 x 128 CTA-pair tiles (x3) when there are
+// at least two waves of 128 x 128 tiles; 128 x 128 tiles when they fill the
 // SMs; else
 // 128 x 64 tiles; and when even those leave half the SMs idle, split-K
 // slices of at least 4 k-blocks.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
   const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
-  const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
-  if (g.k > 0 && pair_tiles_enabled() && 2 * t256 >= (sm / 2) && g.m >= 2 * kTcBM && g.n >= kPair2BN)
+  if (split_bf16_pair256_fits(g, sm))
     return pieces == 2 ? split_gemm_run<128, 2>(h, g, 1, 0, 2) : split_gemm_run<128, 3>(h, g, 1, 0, 2);
   if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) return split_gemm_run<128, 2>(h, g, 1, 0, 1);
   if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 2);
