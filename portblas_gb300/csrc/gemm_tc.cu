@@ -1083,21 +1083,27 @@ static bool pair_tiles_enabled() {
 }
 
 // 256 x 256 CTA-pair tiles: M and N at least 256, tiles for at least half
-// of the resident clusters, and their rounds filled at least 0.8 x as well
-// as those of 128 x 128 one-CTA tiles (the pair tile's MMA rate per SM is
-// about 1.3 x higher).  x3 / x6 TFLOP/s against the next choice: 2048^3 267 /
-// 185 against 225 / 170, 3072^3 430 / 250 against 358 / 208, 6144^3 572 /
-// 308 against 452 / 252; 2304^3 (81 tiles: a second round of 5) and 2560^3
-// (100) ran 2-4% slower on the pair tiles, and the fill rule leaves them out.
+// of the resident clusters, and useful work per round (the rounds' fill
+// times the share of each tile inside the problem) at least 0.8 x that of
+// 128 x 128 one-CTA tiles (the pair tile's MMA rate per SM is about 1.3 x
+// higher).  x3 / x6 TFLOP/s against the next choice: 2048^3 267 / 185
+// against 225 / 170, 3072^3 430 / 250 against 358 / 208, 6144^3 572 / 308
+// against 452 / 252; 2304^3 (81 tiles: a second round of 5) and 2560^3 (100)
+// ran 2-4% slower on the pair tiles, and strided batches of 384^3 and 300^3
+// (tiles a quarter to two thirds padding) 7-9% slower: the rule leaves those out.
 bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm) {
   if (g.k <= 0 || g.m < 2 * kTcBM || g.n < kPair2BN || !pair_tiles_enabled()) return false;
   const int64_t clusters = sm / 2;
-  const int64_t t256 = cdiv(g.m, 2 * kTcBM) * cdiv(g.n, kPair2BN) * g.batch;
-  const int64_t t128 = cdiv(g.m, kTcBM) * cdiv(g.n, 128) * g.batch;
+  const int64_t m256 = cdiv(g.m, 2 * kTcBM), n256 = cdiv(g.n, kPair2BN);
+  const int64_t m128 = cdiv(g.m, kTcBM), n128 = cdiv(g.n, 128);
+  const int64_t t256 = m256 * n256 * g.batch, t128 = m128 * n128 * g.batch;
   if (clusters < 1 || 2 * t256 < clusters) return false;
+  const double mn = double(g.m) * double(g.n);
+  const double use256 = mn / (double(m256 * 2 * kTcBM) * double(n256 * kPair2BN));
+  const double use128 = mn / (double(m128 * kTcBM) * double(n128 * 128));
   const double fill256 = double(t256) / double(cdiv(t256, clusters) * clusters);
   const double fill128 = double(t128) / double(cdiv(t128, sm) * sm);
-  return fill256 >= 0.8 * fill128;
+  return fill256 * use256 >= 0.8 * fill128 * use128;
 }
 
 // The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) where
