@@ -509,7 +509,8 @@ static void plan_tc_operands(int dtype, std::vector<GroupedProblem>& tab, std::v
         o.off = term_bytes;
         term_bytes += (size_t(o.Kp) * size_t(o.k) * 2 + 255) & ~size_t(255);
       } else if (!o.direct && !o.mn) {
-        o.Kp = cdiv(o.k, int64_t(16)) * 16;
+        // FP32: k-block-major terms in 32-deep blocks (gt_term3_ptr)
+        o.Kp = cdiv(o.k, int64_t(P == 3 ? 32 : 16)) * (P == 3 ? 32 : 16);
         o.off = term_bytes;
         term_bytes += (size_t(P) * size_t(o.rows) * size_t(o.Kp) * 2 + 255) & ~size_t(255);
         o.sr = which == 0 ? (p.ta ? p.lda : 1) : (p.tb ? 1 : p.ldb);
@@ -572,11 +573,20 @@ static gbblas_status_t encode_tc_operands(int dtype, const std::vector<GroupedPr
       strides[1] = cuuint64_t(o.sr) * 2 * cuuint64_t(o.rows);
     } else {
       base = terms + o.off;
-      dims[0] = cuuint64_t(o.Kp);
-      dims[1] = cuuint64_t(o.rows);
-      dims[2] = cuuint64_t(P);
-      strides[0] = cuuint64_t(o.Kp) * 2;
-      strides[1] = cuuint64_t(o.Kp) * 2 * cuuint64_t(o.rows);
+      if (P == 3) {
+        // [Kp / 32][3][rows][32]: planes (k-block, term) of rows x 64 bytes
+        dims[0] = cuuint64_t(bk);
+        dims[1] = cuuint64_t(o.rows);
+        dims[2] = cuuint64_t(P) * cuuint64_t(o.Kp / bk);
+        strides[0] = cuuint64_t(bk) * 2;
+        strides[1] = cuuint64_t(bk) * 2 * cuuint64_t(o.rows);
+      } else {
+        dims[0] = cuuint64_t(o.Kp);
+        dims[1] = cuuint64_t(o.rows);
+        dims[2] = cuuint64_t(P);
+        strides[0] = cuuint64_t(o.Kp) * 2;
+        strides[1] = cuuint64_t(o.Kp) * 2 * cuuint64_t(o.rows);
+      }
       box[2] = cuuint32_t(P);
       GtOperand g;
       g.src = o.src;

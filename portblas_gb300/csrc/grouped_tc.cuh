@@ -84,8 +84,10 @@ struct GtCfg {
 };
 
 // One operand to convert: X(r, k) = src[r*sr + k*sk], r < rows, k < K,
-// written as out[p][r][k] for k < Kp (zeros for k >= K; Kp a multiple of 16
-// so every term row starts on a 32-byte sector).
+// written for k < Kp (zeros for k >= K): BF16 as out[r][k] (Kp a multiple of
+// 16, so every row starts on a 32-byte sector), FP32's three terms
+// k-block-major as out[k / 32][p][r][k % 32] (Kp a multiple of 32;
+// gt_term3_ptr).
 struct GtOperand {
   const void* src;
   int64_t sr, sk;
@@ -107,6 +109,15 @@ constexpr int kGtFlat = 4096;
 __host__ __device__ inline int64_t gt_split_blocks(int64_t rows, int64_t Kp, bool kcontig, bool flat) {
   if (!kcontig) return ((rows + 63) / 64) * ((Kp + 63) / 64);
   return flat ? (rows * Kp + kGtFlat - 1) / kGtFlat : ((rows + 31) / 32) * ((Kp + 127) / 128);
+}
+
+// Element (term p, row r, k) of an FP32 operand's three BF16 terms, stored
+// k-block-major as [Kp / 32][3][rows][32] (Kp a multiple of 32): the tile
+// kernel's box for one 32-deep k-block (32 k x 128 rows x 3 terms) is then
+// one contiguous run instead of 384 separate 64-byte row pieces.
+__device__ __forceinline__ __nv_bfloat16* gt_term3_ptr(__nv_bfloat16* out, int64_t rows, int64_t r, int64_t k,
+                                                       int p) {
+  return out + (((k >> 5) * 3 + p) * rows + r) * 32 + (k & 31);
 }
 
 template <typename T>
@@ -191,7 +202,6 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
   const T* __restrict__ X = static_cast<const T*>(op.src);
   __nv_bfloat16* __restrict__ out = op.out;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int64_t plane = int64_t(op.rows) * op.Kp;
   if constexpr (sizeof(T) == 2) {
     if (op.sk == 1) {
       // K-contiguous BF16 (its own single term: the raw 16-bit values move):
@@ -254,9 +264,9 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
           if (r < op.rows) {
             uint32_t w[P][2];
             gt_terms<P, 2>(v[i], w);
-            __nv_bfloat16* o = out + r * op.Kp + k;
 #pragma unroll
-            for (int p = 0; p < P; ++p) *reinterpret_cast<uint2*>(o + p * plane) = make_uint2(w[p][0], w[p][1]);
+            for (int p = 0; p < P; ++p)
+              *reinterpret_cast<uint2*>(gt_term3_ptr(out, op.rows, r, k, p)) = make_uint2(w[p][0], w[p][1]);
           }
         }
       }
@@ -325,10 +335,9 @@ __global__ void __launch_bounds__(256, 8) grouped_split_kernel(const GtOperand* 
         for (int e = 0; e < 8; ++e) x[e] = tile[8 * c + e][rr];
         uint32_t w[P][4];
         gt_terms<P, 4>(x, w);
-        __nv_bfloat16* o = out + r * op.Kp + k;
 #pragma unroll
         for (int p = 0; p < P; ++p)
-          *reinterpret_cast<uint4*>(o + p * plane) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+          *reinterpret_cast<uint4*>(gt_term3_ptr(out, op.rows, r, k, p)) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
       }
     }
     __syncthreads();
@@ -564,17 +573,22 @@ __global__ void __launch_bounds__(kGtThreads, 1)
           tc::mbar_arrive_expect_tx(&full[s], Cfg::STAGE);
           uint8_t* st = smem + s * Cfg::STAGE;
           const int kc = (w.kb0 + kb) * Cfg::BK;
-          if (P == 1 && (w.mn & 1)) {  // two boxes of 64 rows: MN-major tile
-            tc::tma_load_3d(st, ma, &full[s], w.m0, kc, 0);
-            tc::tma_load_3d(st + kGtMnAtom, ma, &full[s], w.m0 + kGtMnBox, kc, 0);
+          if (P == 3) {  // k-block-major terms: plane (k-block, term)
+            tc::tma_load_3d(st, ma, &full[s], 0, w.m0, (w.kb0 + kb) * P);
+            tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], 0, w.n0, (w.kb0 + kb) * P);
           } else {
-            tc::tma_load_3d(st, ma, &full[s], kc, w.m0, 0);
-          }
-          if (P == 1 && (w.mn & 2)) {
-            tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], w.n0, kc, 0);
-            tc::tma_load_3d(st + P * Cfg::A_TILE + kGtMnAtom, mb, &full[s], w.n0 + kGtMnBox, kc, 0);
-          } else {
-            tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kc, w.n0, 0);
+            if (w.mn & 1) {  // two boxes of 64 rows: MN-major tile
+              tc::tma_load_3d(st, ma, &full[s], w.m0, kc, 0);
+              tc::tma_load_3d(st + kGtMnAtom, ma, &full[s], w.m0 + kGtMnBox, kc, 0);
+            } else {
+              tc::tma_load_3d(st, ma, &full[s], kc, w.m0, 0);
+            }
+            if (w.mn & 2) {
+              tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], w.n0, kc, 0);
+              tc::tma_load_3d(st + P * Cfg::A_TILE + kGtMnAtom, mb, &full[s], w.n0 + kGtMnBox, kc, 0);
+            } else {
+              tc::tma_load_3d(st + P * Cfg::A_TILE, mb, &full[s], kc, w.n0, 0);
+            }
           }
         }
         if (!ok) break;
