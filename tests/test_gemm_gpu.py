@@ -439,3 +439,32 @@ def test_split_bf16x3_cta_pair_tiles(sb, torch_cuda, ta, tb):
         np.testing.assert_array_equal(blk[m:], c[i * sc:i * sc + ldc * n].reshape(n, ldc).T[m:])
         np.testing.assert_array_equal(out[i * sc + ldc * n:(i + 1) * sc], c[i * sc + ldc * n:(i + 1) * sc])
     sb.check_device_error()
+
+
+@pytest.mark.parametrize("m,n,k,batch", [(512, 512, 512, 16), (2000, 1500, 300, 1)])
+def test_auto_on_pair_tile_shapes(sb, torch_cuda, m, n, k, batch):
+    """AUTO sends shapes that fit 256 x 256 CTA-pair tiles (M, N >= 256,
+    enough tiles, rounds well filled) to the x6 split: a strided batch and a
+    single problem whose tiles stay partly outside it, alpha and beta, every
+    entry of sampled matrices against the oracle at the x6 bound."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    sb.set_sgemm_mode(blas.sgemm_mode_t.auto)
+    g = rng(m + n + k + batch)
+    lda, ldb, ldc = m + 1, k + 2, m + 3
+    sa, sbs, sc = lda * k, ldb * n, ldc * n
+    a = g.uniform(-1, 1, sa * batch).astype(np.float32)
+    b = g.uniform(-1, 1, sbs * batch).astype(np.float32)
+    c = g.uniform(-1, 1, sc * batch).astype(np.float32)
+    cd = to_dev(c, torch)
+    blas._gemm_strided_batched(sb, "n", "n", m, n, k, 1.25, to_dev(a, torch), lda, sa, to_dev(b, torch), ldb, sbs,
+                               -0.5, cd, ldc, sc, batch)
+    out = to_host(cd)
+    for i in sorted({0, batch // 2, batch - 1}):
+        ref = oracle.gemm(False, False, m, n, k, 1.25, a[i * sa:], lda, b[i * sbs:], ldb, -0.5, c[i * sc:], ldc)
+        scale = oracle.gemm_absscale(False, False, m, n, k, 1.25, a[i * sa:], lda, b[i * sbs:], ldb, -0.5,
+                                     c[i * sc:], ldc)
+        blk = out[i * sc:(i + 1) * sc].reshape(n, ldc).T
+        assert (np.abs(blk[:m] - ref) / scale).max() <= norm_bound("split_bf16x6", k), i
+        np.testing.assert_array_equal(blk[m:], c[i * sc:(i + 1) * sc].reshape(n, ldc).T[m:])
+    sb.check_device_error()
