@@ -1113,6 +1113,10 @@ bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm) {
 // 128 x 64 tiles; and when even those leave half the SMs idle, split-K
 // slices of at least 4 k-blocks.
 gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
+  // the kernels take M, N and the k-block count as int (the CTA-pair paths
+  // included)
+  if (g.m > INT32_MAX / 2 || g.n > INT32_MAX / 2 || g.k > INT32_MAX / 2)
+    return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: dimension too large");
   const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
   if (split_bf16_pair256_fits(g, sm))
