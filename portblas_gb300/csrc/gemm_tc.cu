@@ -578,12 +578,31 @@ __device__ __forceinline__ void term_pair6(int q, int& pa, int& pb) {
   pb = kB[q];
 }
 
+// Work item t of the persistent loop: items below `full` (whole rounds of
+// the clusters) are 256 x 256 tiles in pair_tile order; the items after
+// them are the two 256 x 128 halves of each remaining tile, so a short last
+// round is spread over twice as many clusters at half the work each.
+struct Pair2Item {
+  int bz, mp, n0, width;
+};
+__device__ __forceinline__ Pair2Item pair2_item(int t, int whole, int mp_count, int nt_count) {
+  Pair2Item w;
+  const bool half = t >= whole;
+  const int tt = half ? whole + ((t - whole) >> 1) : t;
+  int nt;
+  pair_tile(tt, mp_count, nt_count, w.bz, w.mp, nt);
+  w.width = half ? kPair2BHalf : kPair2BN;
+  w.n0 = nt * kPair2BN + (half ? ((t - whole) & 1) * kPair2BHalf : 0);
+  return w;
+}
+
 template <int P, int STAGES>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
     gemm_split_bf16_pair256_kernel(const __grid_constant__ CUtensorMap tma_a,
-                                   const __grid_constant__ CUtensorMap tma_b, int M, int N, int nk, int tiles,
-                                   float alpha, float beta, float* __restrict__ C, int64_t ldc, int64_t stride_c,
-                                   int* __restrict__ err) {
+                                   const __grid_constant__ CUtensorMap tma_b,
+                                   const __grid_constant__ CUtensorMap tma_b_half, int M, int N, int nk, int whole,
+                                   int items, float alpha, float beta, float* __restrict__ C, int64_t ldc,
+                                   int64_t stride_c, int* __restrict__ err) {
   using Cfg = Pair2Cfg<P, STAGES>;
   const uint32_t rank = tc::cluster_ctarank();  // 0: issues the MMAs
   const int cid = int(blockIdx.x >> 1), clusters = int(gridDim.x >> 1);
@@ -629,10 +648,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
       const uint32_t full0 = tc::mapa_shared(tc::smem_u32(full), 0);
       uint32_t it = 0;
       bool ok = true;
-      for (int t = cid; t < tiles && ok; t += clusters) {
-        int bz, mp, nt;
-        pair_tile(t, mp_count, nt_count, bz, mp, nt);
-        const int m0 = mp * (2 * kTcBM) + int(rank) * kTcBM, n0 = nt * kPair2BN + int(rank) * kPair2BHalf;
+      for (int t = cid; t < items && ok; t += clusters) {
+        const Pair2Item w = pair2_item(t, whole, mp_count, nt_count);
+        const bool narrow = w.width < kPair2BN;  // this CTA loads w.width / 2 B rows
+        const int m0 = w.mp * (2 * kTcBM) + int(rank) * kTcBM, n0 = w.n0 + int(rank) * (w.width / 2);
+        const uint32_t bytes = 2u * uint32_t(P * (Cfg::A_TILE + (narrow ? Cfg::B_TILE / 2 : Cfg::B_TILE)));
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = int(it % STAGES);
           if (!tc::mbar_wait(&empty[s], ((it / STAGES) & 1) ^ 1)) {
@@ -640,15 +660,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
             ok = false;
             break;
           }
-          if (rank == 0) tc::mbar_arrive_expect_tx(&full[s], 2 * Cfg::STAGE);
+          if (rank == 0) tc::mbar_arrive_expect_tx(&full[s], bytes);
           const uint32_t bar = full0 + uint32_t(s) * 8u;
           uint8_t* st = tiles_smem + s * Cfg::STAGE;
 #pragma unroll
           for (int p = 0; p < P; ++p)
-            tc::tma_load_3d_pair(st + p * Cfg::A_TILE, &tma_a, bar, kb * kTcBK, m0, bz * P + p);
+            tc::tma_load_3d_pair(st + p * Cfg::A_TILE, &tma_a, bar, kb * kTcBK, m0, w.bz * P + p);
 #pragma unroll
           for (int p = 0; p < P; ++p)
-            tc::tma_load_3d_pair(st + P * Cfg::A_TILE + p * Cfg::B_TILE, &tma_b, bar, kb * kTcBK, n0, bz * P + p);
+            tc::tma_load_3d_pair(st + P * Cfg::A_TILE + p * Cfg::B_TILE, narrow ? &tma_b_half : &tma_b, bar,
+                                 kb * kTcBK, n0, w.bz * P + p);
         }
       }
       if (rank == 0)
@@ -660,10 +681,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0 && rank == 0) {
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * kTcBM, kPair2BN);
       uint32_t it = 0, g = 0;
       bool ok = true;
-      for (int t = cid; t < tiles && ok; t += clusters) {
+      for (int t = cid; t < items && ok; t += clusters) {
+        const uint32_t idesc = tc::idesc_bf16_f32(2 * kTcBM, t < whole ? kPair2BN : kPair2BHalf);
         for (int c = 0; c < nchunks && ok; ++c, ++g) {
           const int b = int(g % kPair2Acc);
           if (!tc::mbar_wait(&tempty[b], ((g / kPair2Acc) & 1) ^ 1)) {
@@ -707,10 +728,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
     const uint32_t tempty0 = tc::mapa_shared(tc::smem_u32(tempty), 0);
     uint32_t g = 0;
     bool ok = true;
-    for (int t = cid; t < tiles && ok; t += clusters) {
-      int bz, mp, nt;
-      pair_tile(t, mp_count, nt_count, bz, mp, nt);
-      const int gm = mp * (2 * kTcBM) + int(rank) * kTcBM + row, nb = nt * kPair2BN + cg * 64;
+    for (int t = cid; t < items && ok; t += clusters) {
+      const Pair2Item w = pair2_item(t, whole, mp_count, nt_count);
+      const int bz = w.bz;
+      const int gm = w.mp * (2 * kTcBM) + int(rank) * kTcBM + row, nb = w.n0 + cg * 64;
+      // a half-width item's accumulator holds 128 columns: warps past them
+      // drain their share and store nothing
+      const bool cols_in = cg * 64 < w.width;
       float sum[64];
 #pragma unroll
       for (int i = 0; i < 64; ++i) sum[i] = 0.f;
@@ -737,7 +761,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPair2Threads, 1)
         __syncwarp();
         if (lane == 0) tc::mbar_arrive_cluster(tempty0 + uint32_t(b) * 8u);
       }
-      if (ok && gm < M) {
+      if (ok && gm < M && cols_in) {
         float* rowp = C + int64_t(bz) * stride_c + int64_t(gm);
 #pragma unroll
         for (int g0 = 0; g0 < 64; g0 += 8) {
@@ -980,8 +1004,9 @@ static gbblas_status_t launch_tc_pair(gbblas_handle_t h, const CUtensorMap& ta, 
 // resident at once.
 template <int P>
 static gbblas_status_t launch_tc_pair256(gbblas_handle_t h, const CUtensorMap& ta, const CUtensorMap& tb,
-                                         int64_t M, int64_t N, int64_t nk, int64_t batch, float alpha, float beta,
-                                         float* C, int64_t ldc, int64_t stride_c) {
+                                         const CUtensorMap& tb_half, int64_t M, int64_t N, int64_t nk,
+                                         int64_t batch, float alpha, float beta, float* C, int64_t ldc,
+                                         int64_t stride_c) {
   constexpr int STAGES = P == 2 ? 3 : 2;
   using Cfg = Pair2Cfg<P, STAGES>;
   auto* kern = gemm_split_bf16_pair256_kernel<P, STAGES>;
@@ -1008,10 +1033,18 @@ static gbblas_status_t launch_tc_pair256(gbblas_handle_t h, const CUtensorMap& t
     if (clusters < 1) return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: no CTA pair can be resident");
     if (h->device >= 0 && h->device < 64) resident[h->device].store(clusters, std::memory_order_release);
   }
-  const int64_t grid_clusters = std::min<int64_t>(tiles, clusters);
+  // a last round of at most half the clusters runs as 256 x 128 halves
+  // (one per cluster): 8192^3 has 13 rounds of 76 tiles and 36 more
+  int64_t whole = tiles, items = tiles;
+  const int64_t leftover = tiles % clusters;
+  if (tiles > clusters && leftover > 0 && 2 * leftover <= clusters) {
+    whole = tiles - leftover;
+    items = whole + 2 * leftover;
+  }
+  const int64_t grid_clusters = std::min<int64_t>(items, clusters);
   const cudaError_t le = launch_pdl(true, kern, dim3(unsigned(2 * grid_clusters)), dim3(kPair2Threads), Cfg::SMEM,
-                                    h->stream, ta, tb, int(M), int(N), int(nk), int(tiles), alpha, beta, C, ldc,
-                                    stride_c, h->dev_error);
+                                    h->stream, ta, tb, tb_half, int(M), int(N), int(nk), int(whole), int(items),
+                                    alpha, beta, C, ldc, stride_c, h->dev_error);
   if (le != cudaSuccess) return cuda_fail(le, "gemm_split_bf16_pair256");
   return after_launch("gemm_split_bf16_pair256");
 }
@@ -1047,8 +1080,10 @@ static gbblas_status_t split_gemm_run(gbblas_handle_t h, const GemmArgs<float>& 
     return launch_tc_pair(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
   }
   if (pair == 2 && split == 1) {
+    CUtensorMap mbh;  // B rows of a 256 x 128 half item (64 per CTA)
     GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, kPair2BHalf));
-    return launch_tc_pair256<P>(h, ma, mb, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
+    GB_TRY(make_term_map(&mbh, bt, N, Kp, P * B, kPair2BHalf / 2));
+    return launch_tc_pair256<P>(h, ma, mb, mbh, M, N, nk, B, g.alpha, g.beta, g.c, g.ldc, g.stride_c);
   }
   GB_TRY(make_term_map(&mb, bt, N, Kp, P * B, BN));
   if (split == 1)
