@@ -1121,11 +1121,12 @@ static bool pair_tiles_enabled() {
 // of the resident clusters, and useful work per round (the rounds' fill
 // times the share of each tile inside the problem) at least 0.8 x that of
 // 128 x 128 one-CTA tiles (the pair tile's MMA rate per SM is about 1.3 x
-// higher).  x3 / x6 TFLOP/s against the next choice: 2048^3 267 / 185
-// against 225 / 170, 3072^3 430 / 250 against 358 / 208, 6144^3 572 / 308
-// against 452 / 252; 2304^3 (81 tiles: a second round of 5) and 2560^3 (100)
-// ran 2-4% slower on the pair tiles, and strided batches of 384^3 and 300^3
-// (tiles a quarter to two thirds padding) 7-9% slower: the rule leaves those out.
+// higher); a short last round run as 256 x 128 halves counts 0.6 of a
+// round.  x3 / x6 TFLOP/s against the next choice: 2048^3 267 / 185 against
+// 225 / 170, 2560^3 325 / 199 against 292 / 183, 3072^3 430 / 250 against
+// 358 / 208, 6144^3 572 / 308 against 452 / 252; strided batches of 384^3
+// and 300^3 (tiles a quarter to two thirds padding) ran 7-9% slower on the
+// pair tiles, and the rule leaves them out.
 bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm) {
   if (g.k <= 0 || g.m < 2 * kTcBM || g.n < kPair2BN || !pair_tiles_enabled()) return false;
   const int64_t clusters = sm / 2;
@@ -1136,7 +1137,12 @@ bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm) {
   const double mn = double(g.m) * double(g.n);
   const double use256 = mn / (double(m256 * 2 * kTcBM) * double(n256 * kPair2BN));
   const double use128 = mn / (double(m128 * kTcBM) * double(n128 * 128));
-  const double fill256 = double(t256) / double(cdiv(t256, clusters) * clusters);
+  // a last round of at most half the clusters runs as 256 x 128 halves,
+  // about 0.6 of a round
+  const int64_t left = t256 % clusters, whole_rounds = t256 / clusters;
+  const double rounds = double(whole_rounds) +
+                        (left == 0 ? 0.0 : (whole_rounds > 0 && 2 * left <= clusters ? 0.6 : 1.0));
+  const double fill256 = double(t256) / (rounds * double(clusters));
   const double fill128 = double(t128) / double(cdiv(t128, sm) * sm);
   return fill256 * use256 >= 0.8 * fill128 * use128;
 }
