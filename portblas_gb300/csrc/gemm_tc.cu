@@ -549,8 +549,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
 // the work for the same A read; every term product of a TMEM chunk goes into
 // one accumulator (two of 256 columns, so the MMAs of the next chunk run
 // while the epilogue promotes this one); sixteen epilogue warps per CTA, four
-// per TMEM lane quarter, each with 64 of the 256 columns.  Used where the
-// 256 x 256 tiles fill at least half of the resident clusters.
+// per TMEM lane quarter, each with 64 of the 256 columns.  A short last
+// round (at most half the clusters) runs as 256 x 128 halves of its tiles
+// (pair2_item): each CTA loads 64 B rows through a second tensor map, the
+// MMA is N = 128 and the epilogue warps past column 128 store nothing.
+// Used where the 256 x 256 tiles fill at least half of the resident
+// clusters.
 constexpr int kPair2BN = 256, kPair2BHalf = kPair2BN / 2;
 constexpr int kPair2EpiWarps = 16, kPair2Threads = 32 * (2 + kPair2EpiWarps);
 constexpr int kPair2Acc = 2;
