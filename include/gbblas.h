@@ -300,6 +300,14 @@ gbblas_status_t gbblas_gemm_selector_pick(int dtype, int64_t m, int64_t n, int64
                                           int64_t lda, int64_t ldb, int64_t ldc, int64_t batch, int* config);
 gbblas_status_t gbblas_sgemm_selector_pick(int64_t m, int64_t n, int64_t k, char transa, char transb, int64_t lda,
                                            int64_t ldb, int64_t ldc, int64_t batch, int* config);
+/* No portBLAS counterpart: the tiles the fixed split-BF16 modes (`mode`
+ * GBBLAS_SGEMM_SPLIT_BF16X3 or _X6) run an m x n x k GEMM of `batch`
+ * matrices on, for a GPU with `sm_count` SMs, computed on the host (no device
+ * call).  `tile_m` x `tile_n`: the output tile of one work item (tile_m 256:
+ * a CTA pair sharing one tile); `k_slices`: split-K slices (1: no split).
+ * Any output pointer may be null. */
+gbblas_status_t gbblas_sgemm_split_route(int64_t m, int64_t n, int64_t k, int64_t batch, int mode, int sm_count,
+                                         int* tile_m, int* tile_n, int* k_slices);
 /* Exhaustive autotune of one shape: times every config of the element type
  * (`reps` launches each) on zero-filled operands, remembers the winner for
  * AUTO. */

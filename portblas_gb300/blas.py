@@ -391,6 +391,17 @@ def _gemm_grouped(sb_handle, problems, dtype="float32"):
     return _call("gbblas_gemm_grouped", sb_handle.handle, _dtype_code(dtype), *args)
 
 
+def sgemm_split_route(m, n, k, batch=1, mode=sgemm_mode_t.split_bf16x3, sm_count=152):
+    """Host-side tile choice of the fixed split-BF16 modes for an m x n x k
+    GEMM of ``batch`` matrices on a GPU with ``sm_count`` SMs:
+    (tile_m, tile_n, k_slices); tile_m 256 is a CTA pair sharing one tile."""
+    L = _lib.load()
+    tm, tn, ks = C.c_int(), C.c_int(), C.c_int()
+    _check(L.gbblas_sgemm_split_route(int(m), int(n), int(k), int(batch), int(mode), int(sm_count), C.byref(tm),
+                                      C.byref(tn), C.byref(ks)))
+    return tm.value, tn.value, ks.value
+
+
 def grouped_schedule(problems, dtype="float32", sm_count=152):
     """Host-side tile schedule of a tcgen05 grouped GEMM over ``problems``
     (dicts with transa, transb, m, n, k, alpha) on a GPU with ``sm_count``

@@ -52,6 +52,13 @@ gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>&
 // The fixed split-BF16 modes take 256 x 256 CTA-pair tiles for this shape
 // (M and N at least 256, enough tiles, the last round filled well enough).
 bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm_count);
+// The tiles launch_gemm_split_bf16 runs this shape on (pieces: 2 = x3,
+// 3 = x6): output tile tile_m x tile_n (tile_m 256: a CTA pair) and the
+// number of split-K slices.
+struct SplitBf16Route {
+  int tile_m, tile_n, k_slices;
+};
+SplitBf16Route split_bf16_route(const GemmArgs<float>& g, int pieces, int64_t sm_count);
 // Same with an explicit N tile (64 or 128), split-K factor and raster order
 // (raster_m: consecutive CTAs walk down M).
 gbblas_status_t launch_gemm_split_bf16_cfg(gbblas_handle_t h, const GemmArgs<float>& g, int pieces, int bn,

@@ -1154,20 +1154,14 @@ bool split_bf16_pair256_fits(const GemmArgs<float>& g, int64_t sm) {
 // The fixed split-BF16 modes: 256 x 256 CTA-pair tiles (x3 and x6) where
 // split_bf16_pair256_fits; else 256 x 128 CTA-pair tiles (x3) when there are
 // at least two waves of 128 x 128 tiles; 128 x 128 tiles when they fill the
-// SMs; else
-// 128 x 64 tiles; and when even those leave half the SMs idle, split-K
-// slices of at least 4 k-blocks.
-gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
-  // the kernels take M, N and the k-block count as int (the CTA-pair paths
-  // included)
-  if (g.m > INT32_MAX / 2 || g.n > INT32_MAX / 2 || g.k > INT32_MAX / 2)
-    return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: dimension too large");
-  const int64_t sm = h->sm_count, tm = cdiv(g.m, kTcBM);
+// SMs; else 128 x 64 tiles; and when even those leave half the SMs idle,
+// split-K slices of at least 4 k-blocks.
+SplitBf16Route split_bf16_route(const GemmArgs<float>& g, int pieces, int64_t sm) {
+  if (split_bf16_pair256_fits(g, sm)) return {2 * kTcBM, kPair2BN, 1};
+  const int64_t tm = cdiv(g.m, kTcBM);
   const int64_t t128 = tm * cdiv(g.n, 128) * g.batch;
-  if (split_bf16_pair256_fits(g, sm))
-    return pieces == 2 ? split_gemm_run<128, 2>(h, g, 1, 0, 2) : split_gemm_run<128, 3>(h, g, 1, 0, 2);
-  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) return split_gemm_run<128, 2>(h, g, 1, 0, 1);
-  if (t128 >= sm || g.n <= 64) return launch_gemm_split_bf16_cfg(h, g, pieces, 128, 1, 2);
+  if (pieces == 2 && t128 >= 2 * sm && g.k > 0 && pair_tiles_enabled()) return {2 * kTcBM, 128, 1};
+  if (t128 >= sm || g.n <= 64) return {kTcBM, 128, 1};
   const int64_t t64 = tm * cdiv(g.n, 64) * g.batch;
   int64_t split = 1;
   if (2 * t64 <= sm) {
@@ -1177,7 +1171,49 @@ gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>&
     if (split > 16) split = 16;
     if (split < 1) split = 1;
   }
-  return launch_gemm_split_bf16_cfg(h, g, pieces, 64, int(split), 0);
+  return {kTcBM, 64, int(split)};
+}
+
+gbblas_status_t launch_gemm_split_bf16(gbblas_handle_t h, const GemmArgs<float>& g, int pieces) {
+  // the kernels take M, N and the k-block count as int (the CTA-pair paths
+  // included)
+  if (g.m > INT32_MAX / 2 || g.n > INT32_MAX / 2 || g.k > INT32_MAX / 2)
+    return fail(GBBLAS_STATUS_UNSUPPORTED, "split-BF16 GEMM: dimension too large");
+  const SplitBf16Route r = split_bf16_route(g, pieces, h->sm_count);
+  if (r.tile_m == 2 * kTcBM) {
+    if (r.tile_n == kPair2BN)
+      return pieces == 2 ? split_gemm_run<128, 2>(h, g, 1, 0, 2) : split_gemm_run<128, 3>(h, g, 1, 0, 2);
+    return split_gemm_run<128, 2>(h, g, 1, 0, 1);
+  }
+  return launch_gemm_split_bf16_cfg(h, g, pieces, r.tile_n, r.k_slices, r.tile_n == 128 ? 2 : 0);
 }
 
 }  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+gbblas_status_t gbblas_sgemm_split_route(int64_t m, int64_t n, int64_t k, int64_t batch, int mode, int sm_count,
+                                         int* tile_m, int* tile_n, int* k_slices) {
+  clear_error();
+  if (m < 0 || n < 0 || k < 0 || batch < 0)
+    return fail(GBBLAS_STATUS_INVALID_ARG, "sgemm_split_route: negative dimension");
+  if (mode != GBBLAS_SGEMM_SPLIT_BF16X3 && mode != GBBLAS_SGEMM_SPLIT_BF16X6)
+    return fail(GBBLAS_STATUS_INVALID_ARG, "sgemm_split_route: mode must be SPLIT_BF16X3 or SPLIT_BF16X6");
+  if (sm_count < 1) return fail(GBBLAS_STATUS_INVALID_ARG, "sgemm_split_route: sm_count must be positive");
+  if (m > INT32_MAX / 2 || n > INT32_MAX / 2 || k > INT32_MAX / 2)
+    return fail(GBBLAS_STATUS_UNSUPPORTED, "sgemm_split_route: dimension too large");
+  GemmArgs<float> g{};
+  g.m = m;
+  g.n = n;
+  g.k = k;
+  g.batch = batch;
+  const SplitBf16Route r = split_bf16_route(g, mode == GBBLAS_SGEMM_SPLIT_BF16X3 ? 2 : 3, sm_count);
+  if (tile_m) *tile_m = r.tile_m;
+  if (tile_n) *tile_n = r.tile_n;
+  if (k_slices) *k_slices = r.k_slices;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+}  // extern "C"
