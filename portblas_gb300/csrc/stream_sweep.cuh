@@ -417,21 +417,60 @@ struct TmaPlan {
   bool full_wave;                   // the grid fills (nearly) every resident slot: launched early (PDL)
 };
 
-// rows sweep: 3 resident CTAs per SM
-inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes) {
+// rows sweep: first the split that fills one wave of 3 CTAs per SM; it is
+// kept when its grid is resident at once with at least 2 CTAs on every SM
+// (the resident CTAs per SM, at most 3, counted from the shared memory a CTA
+// of that split takes, x staged or not).  Otherwise the split that
+// minimises (waves of resident CTAs) x (tiles per CTA + 4): a last wave of
+// few CTAs leaves HBM idle for the length of a whole CTA, and the 4 tiles
+// stand for a CTA's start (ring fill, first-load latency).  GEMV 'n' GB/s,
+// one-wave split -> this one (split in brackets): 16384^2 6139 (3: x staged,
+// so 2 CTAs per SM and 1.26 waves) -> 6800 (14), 30000^2 3762 (1: 235 CTAs)
+// -> 7140 (21), 40000 x 8192 5374 (1) -> 6876 (7); 8192^2 and the 16384^2
+// outer reduction keep their one-wave splits (7 and 3; the cost rule's 7 for
+// the reduction measured 1% slower).
+constexpr int64_t kSmemPerSm = 233472;  // shared memory of one SM (sm_103a), bytes
+constexpr int64_t kSmemPerCta = 1024;   // reserved by the system per resident CTA
+constexpr int64_t kRowsMaxSplit = 64;
+
+inline TmaPlan plan_rows_tma(int64_t M, int64_t N, int sm_count, int elem_bytes, int64_t smem_base, bool has_x) {
   const int64_t BM = 512 / elem_bytes, BC = kStTileBytes / 512;
-  const int64_t slots = int64_t(sm_count) * 3;
   TmaPlan p;
   p.tiles = cdiv(M, BM);
-  // fill the 3 resident CTAs per SM in one wave
-  int64_t split = slots / p.tiles;
-  const int64_t max_split = cdiv(N, 4 * BC);  // at least 4 tiles per CTA
-  if (split > max_split) split = max_split;
-  if (split < 1 || p.tiles > int64_t(kMaxTickets)) split = 1;
-  p.per_split = cdiv(cdiv(N, split), BC) * BC;
+  const int64_t ct = cdiv(N, BC);
+  int64_t max_split = cdiv(N, 4 * BC);  // at least 4 tiles per CTA
+  if (p.tiles > int64_t(kMaxTickets)) max_split = 1;
+  if (max_split > kRowsMaxSplit) max_split = kRowsMaxSplit;
+  // resident slots of a split of `per` tiles per CTA
+  auto slots_of = [&](int64_t per) {
+    const int64_t cols = per * BC;
+    const int64_t smem = smem_base + ((has_x && cols <= kRowsXStage) ? elem_bytes * cols : 0);
+    int64_t per_sm = kSmemPerSm / (smem + kSmemPerCta);
+    if (per_sm > 3) per_sm = 3;
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * sm_count;
+  };
+  int64_t s0 = 3 * int64_t(sm_count) / p.tiles;
+  if (s0 > max_split) s0 = max_split;
+  if (s0 < 1) s0 = 1;
+  int64_t best_per = cdiv(ct, s0), best_slots = slots_of(best_per);
+  const int64_t grid0 = p.tiles * cdiv(ct, best_per);
+  if (!(grid0 <= best_slots && grid0 >= 2 * int64_t(sm_count))) {
+    double best = -1.0;
+    for (int64_t s = 1; s <= max_split; ++s) {
+      const int64_t per = cdiv(ct, s), slots = slots_of(per);
+      const double cost = double(cdiv(p.tiles * cdiv(ct, per), slots)) * double(per + 4);
+      if (best < 0.0 || cost < best) {
+        best = cost;
+        best_per = per;
+        best_slots = slots;
+      }
+    }
+  }
+  p.per_split = best_per * BC;
   p.split = cdiv(N, p.per_split);
   const int64_t grid = p.tiles * p.split;
-  p.full_wave = grid <= slots && 32 * grid >= 31 * slots;
+  p.full_wave = grid <= best_slots && 32 * grid >= 31 * best_slots;
   return p;
 }
 
@@ -473,7 +512,7 @@ inline bool try_rows_sweep_tma(gbblas_handle_t h, const P& pol, int64_t M, int64
   constexpr int BM = 512 / int(sizeof(T));
   constexpr int BC = kStTileBytes / 512;
   if (M < BM || N < 4 * BC) return false;
-  TmaPlan p = plan_rows_tma(M, N, h->sm_count, sizeof(T));
+  TmaPlan p = plan_rows_tma(M, N, h->sm_count, int(sizeof(T)), int64_t(rows_tma_smem<Acc, T>(false)), HAS_X);
   if (p.split > 65535 || p.tiles > INT32_MAX) return false;
   CUtensorMap map;
   if (!make_matrix_map(&map, A, M, N, lda, BM, BC)) return false;

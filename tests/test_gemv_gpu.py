@@ -80,11 +80,13 @@ def test_gemv_full_size_linearity(sb, torch_cuda, trans):
 
 @pytest.mark.parametrize("trans", ["n", "t"])
 @pytest.mark.parametrize("m,n,lda", [(1000, 700, 1000), (4100, 300, 4104), (520, 1030, 520), (8192, 257, 8192),
-                                     (257, 5000, 260)])
+                                     (257, 5000, 260), (30000, 2048, 30000)])
 @pytest.mark.parametrize("beta", [0.0, 0.5])
 def test_gemv_tma_stream_path(sb, torch_cuda, trans, m, n, lda, beta):
     """Shapes whose lda satisfies the tensor-map rules take the TMA-fed sweeps:
-    ragged row/column tiles, split combines, strided x/y."""
+    ragged row/column tiles, split combines, strided x/y.  30000 x 2048 'n':
+    235 row tiles, fewer than two per SM in one wave, so the column split
+    comes from the wave cost (3 splits of 22, 22 and 20 tiles)."""
     torch = torch_cuda
     from portblas_gb300 import blas
     g = rng(m + n + lda)
