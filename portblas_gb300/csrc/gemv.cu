@@ -29,6 +29,35 @@ struct GemvPolicy {
   }
 };
 
+// GEMV 'n' with at most kNarrowRows rows: rows_narrow over about four CTAs
+// per SM, each over at least four whole load rounds of columns.
+template <typename T>
+static gbblas_status_t gemv_n_narrow(gbblas_handle_t h, const GemvPolicy<T>& pol, int64_t m, int64_t n,
+                                     const T* a, int64_t lda, const T* xb, int64_t incx, bool vec) {
+  constexpr int RPT = 16 / sizeof(T);
+  int lpc_log2 = 0;
+  while ((int64_t(1) << lpc_log2) * RPT < m) ++lpc_log2;
+  const int64_t round = int64_t(32 >> lpc_log2) * kMvWarps;  // columns of one load round of a CTA
+  const int64_t cols = n > 0 ? n : 1;
+  int64_t per = cdiv(cdiv(cols, 4 * int64_t(h->sm_count)), round) * round;
+  if (per < 4 * round) per = 4 * round;
+  const int64_t grid = cdiv(cols, per);
+  if (grid > INT32_MAX) return fail(GBBLAS_STATUS_UNSUPPORTED, "gemv: too many columns");
+  T* partials = nullptr;
+  if (grid > 1) {
+    void* tmp;
+    GB_TRY(temp_acquire(h, sizeof(T) * grid * m, &tmp));
+    partials = static_cast<T*>(tmp);
+  }
+  if (vec)
+    rows_narrow<GemvPolicy<T>, T, true, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(
+        pol, int(m), n, a, lda, xb, incx, lpc_log2, per, partials, h->tickets);
+  else
+    rows_narrow<GemvPolicy<T>, T, false, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(
+        pol, int(m), n, a, lda, xb, incx, lpc_log2, per, partials, h->tickets);
+  return after_launch("gemv_n_narrow");
+}
+
 template <typename T>
 gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T alpha, const T* a, int64_t lda,
                           const T* x, int64_t incx, T beta, T* y, int64_t incy) {
@@ -47,6 +76,7 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
   if (!tr) {
     gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
     if (try_rows_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;
+    if (m <= kNarrowRows) return gemv_n_narrow<T>(h, pol, m, n, a, lda, xb, incx, vec);
     SweepPlan p = plan_rows(m, n, h->sm_count, sizeof(T));
     T* partials = nullptr;
     if (p.split > 1) {
@@ -62,6 +92,18 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
       rows_sweep<GemvPolicy<T>, T, false, true><<<grid, kMvThreads, 0, h->stream>>>(
           pol, m, n, a, lda, xb, incx, p.per_split, partials, h->tickets);
     return after_launch("gemv_n");
+  }
+  if (m <= kNarrowRows) {
+    // at most kNarrowRows rows: one thread per column (cols_thread)
+    const int64_t grid = cdiv(n, kMvThreads);
+    if (grid > INT32_MAX) return fail(GBBLAS_STATUS_UNSUPPORTED, "gemv: too many columns");
+    if (vec)
+      cols_thread<GemvPolicy<T>, T, true, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, int(m), n, a,
+                                                                                               lda, xb, incx);
+    else
+      cols_thread<GemvPolicy<T>, T, false, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, int(m), n, a,
+                                                                                                lda, xb, incx);
+    return after_launch("gemv_t_narrow");
   }
   {
     // aligned columns up to two per warp of the wave: a CTA per column

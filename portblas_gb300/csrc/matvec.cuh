@@ -311,6 +311,145 @@ __global__ void __launch_bounds__(kMvThreads, 4)
   if (t == 0) tickets[rblock] = 0u;
 }
 
+// ------------------------------------------------------------ narrow rows --
+// Matrices of at most kNarrowRows rows (short and wide).  One warp-wide
+// load of the sweeps above covers 32 x (16 / sizeof(T)) rows of ONE column,
+// so with 8 rows a warp read 32 useful bytes per load and GEMV 'n' 8 x 2^22
+// ran at 356 GB/s.  Here a column takes `lpc` lanes (rows / RPT rounded up to
+// a power of two) and a warp covers 32 / lpc columns per load: a packed A
+// (lda == rows) streams in contiguous 512-byte warp loads.
+constexpr int kNarrowRows = 32;
+
+// out(i) = fold over j of pol.add(A[i + j*lda], x[j]), i < M <= kNarrowRows.
+// CTA b takes columns [b*cols_per_cta, ...); lanes with the same row group
+// are folded by shuffles, warps in warp order in shared memory, and the
+// CTAs' per-row partials by the last CTA to finish, all 256 threads over
+// equal runs of CTAs, then the runs in order.
+template <class P, typename T, bool VEC, bool HAS_X>
+__global__ void __launch_bounds__(kMvThreads)
+    rows_narrow(P pol, int M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
+                int64_t incx, int lpc_log2, int64_t cols_per_cta, typename P::Acc* __restrict__ partials,
+                unsigned int* __restrict__ tickets) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  __shared__ Acc red[kMvThreads];  // [warp][32 rows], later [run][row]
+  __shared__ bool is_last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lpc = 1 << lpc_log2, cpw = 32 >> lpc_log2;
+  const int r0 = (lane & (lpc - 1)) * RPT;
+  const int64_t c0 = int64_t(blockIdx.x) * cols_per_cta;
+  const int64_t c1 = min(N, c0 + cols_per_cta);
+  const int64_t step = int64_t(cpw) * kMvWarps;
+  const bool full = VEC && r0 + RPT <= M;
+  Acc acc[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
+  auto load_col = [&](int64_t j, T* v) {
+    const T* col = A + j * lda + r0;
+    if (full) {
+      Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(col)), v);
+    } else {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) v[r] = r0 + r < M ? col[r] : T(0);
+    }
+  };
+  int64_t j = c0 + warp * cpw + (lane >> lpc_log2);
+  constexpr int U = 4;
+  for (; j + (U - 1) * step < c1; j += U * step) {
+    T v[U][RPT];
+    T xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      load_col(j + u * step, v[u]);
+      xv[u] = HAS_X ? xb[(j + u * step) * incx] : T(1);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[u][r], xv[u]);
+  }
+  for (; j < c1; j += step) {
+    T v[RPT];
+    load_col(j, v);
+    const T xv = HAS_X ? xb[j * incx] : T(1);
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[r], xv);
+  }
+  // lanes l, l + lpc, l + 2 lpc, ... hold the same rows: fold them into lane l
+  for (int off = 16; off >= lpc; off >>= 1)
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) pol.merge(acc[r], pol.shfl_down(acc[r], off));
+  if (lane < lpc)
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) red[warp * 32 + r0 + r] = acc[r];
+  __syncthreads();
+  const int t = threadIdx.x;
+  Acc s;
+  if (t < M) {
+    s = red[t];
+    for (int w = 1; w < kMvWarps; ++w) pol.merge(s, red[w * 32 + t]);
+  }
+  if (gridDim.x == 1) {
+    if (t < M) pol.finish(s, t);
+    return;
+  }
+  if (t < M) partials[int64_t(blockIdx.x) * M + t] = s;
+  __threadfence();
+  __syncthreads();
+  if (t == 0) is_last = atomicAdd(tickets, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  const int runs = kMvThreads / M;
+  const int64_t per = (int64_t(gridDim.x) + runs - 1) / runs;
+  if (t < runs * M) {
+    const int row = t % M, run = t / M;
+    const int64_t b0 = run * per, b1 = min(int64_t(gridDim.x), b0 + per);
+    Acc f = pol.init();
+    for (int64_t b = b0; b < b1; ++b) pol.merge(f, ldcg_any(partials + b * M + row));
+    red[run * M + row] = f;
+  }
+  __syncthreads();
+  if (t < M) {
+    Acc f = red[t];
+    for (int run = 1; run < runs; ++run) pol.merge(f, red[run * M + t]);
+    pol.finish(f, t);
+  }
+  if (t == 0) tickets[0] = 0u;
+}
+
+// out(j) = fold over i < M of pol.add(A[i + j*lda], x[i]), M <= kNarrowRows:
+// one thread per column, its M values in at most 8 (FP32) 16-byte loads; x
+// in shared memory.  A packed A streams as contiguous 1 KB warp loads (8 x
+// 2^22 GEMV 't' ran at 221 GB/s with a warp per column).
+template <class P, typename T, bool VEC, bool HAS_X>
+__global__ void __launch_bounds__(kMvThreads)
+    cols_thread(P pol, int M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
+                int64_t incx) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  __shared__ T xs[kNarrowRows];
+  if (threadIdx.x < M) xs[threadIdx.x] = HAS_X ? xb[int64_t(threadIdx.x) * incx] : T(1);
+  __syncthreads();
+  const int64_t j = int64_t(blockIdx.x) * kMvThreads + threadIdx.x;
+  if (j >= N) return;
+  const T* col = A + j * lda;
+  Acc acc = pol.init();
+  if (VEC) {
+    int i = 0;
+    for (; i + RPT <= M; i += RPT) {
+      T v[RPT];
+      Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(col + i)), v);
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) pol.add(acc, v[r], xs[i + r]);
+    }
+    for (; i < M; ++i) pol.add(acc, col[i], xs[i]);
+  } else {
+    for (int i = 0; i < M; ++i) pol.add(acc, col[i], xs[i]);
+  }
+  pol.finish(acc, j);
+}
+
 // ------------------------------------------------------------- cols sweep --
 // CTA = 8 warps over CC columns and one chunk of `rows_per_split` rows; x of
 // the chunk is staged in shared memory; warp w takes columns w, w+8, ... and

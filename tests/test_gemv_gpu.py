@@ -152,3 +152,39 @@ def test_gemv_t_warp_per_column_misaligned(sb, torch_cuda, m, n, lda, off):
     ad, xd, yd = to_dev(a, torch), to_dev(x, torch), to_dev(y, torch)
     blas._gemv(sb, "t", m, n, 0.75, ad[off:], lda, xd[off:], 1, 0.5, yd, 1)
     np.testing.assert_allclose(to_host(yd), ref, rtol=2e-5, atol=2e-5 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+@pytest.mark.parametrize("m,n,lda,incx,incy", [(8, 1 << 22, 8, 1, 1), (3, 70001, 3, 1, 1), (32, 20000, 32, 2, 3),
+                                               (17, 5003, 20, -1, 2), (1, 9000, 1, 1, 1), (5, 64, 7, 3, 1),
+                                               (32, 1, 32, 1, 1), (12, 0, 12, 1, 1)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_gemv_narrow_rows(sb, torch_cuda, trans, m, n, lda, incx, incy, dtype):
+    """At most 32 rows: 'n' runs rows_narrow (several columns per warp load,
+    the CTAs' partials folded by the last CTA), 't' runs cols_thread (one
+    thread per column); packed, padded and odd leading dimensions, strided
+    and reversed x, strided y, no columns at all."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(m + n + lda + int(dtype == np.float64))
+    a = g.uniform(-1, 1, max(lda * n, 1)).astype(dtype)
+    xlen, ylen = (n, m) if trans == "n" else (m, n)
+    if ylen == 0:
+        pytest.skip("no output")
+    x = g.uniform(-1, 1, max(xlen * abs(incx), 1)).astype(dtype)
+    y = g.uniform(-1, 1, ylen * incy).astype(dtype)
+    ref = oracle.gemv(trans, m, n, 0.75, a, lda, x, incx, 0.5, y, incy)
+    yd = to_dev(y, torch)
+    blas._gemv(sb, trans, m, n, 0.75, to_dev(a, torch), lda, to_dev(x, torch), incx, 0.5, yd, incy)
+    out = to_host(yd)
+    got = oracle.view(out, ylen, incy)
+    # error against the FP64 oracle, normalised by |alpha| |op(A)| |x| + |beta| |y|
+    A2 = a[:lda * n].reshape(n, lda)[:, :m].astype(np.float64).T
+    xv = np.abs(oracle.view(x, xlen, incx).astype(np.float64))
+    scale = 0.75 * (np.abs(A2) @ xv if trans == "n" else np.abs(A2).T @ xv)
+    scale = scale + 0.5 * np.abs(oracle.view(y, ylen, incy).astype(np.float64))
+    assert (np.abs(got - ref) / scale).max() <= 256 * np.finfo(dtype).eps
+    mask = np.ones(len(y), bool)
+    mask[: ylen * incy: incy] = False
+    np.testing.assert_array_equal(out[mask], y[mask])
+    sb.check_device_error()
