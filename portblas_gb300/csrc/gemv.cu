@@ -29,7 +29,7 @@ struct GemvPolicy {
   }
 };
 
-// GEMV 'n' with at most kNarrowRows rows: rows_narrow over about four CTAs
+// GEMV 'n' with at most narrow_rows<T>() rows: rows_narrow over about four CTAs
 // per SM, each over at least four whole load rounds of columns.
 template <typename T>
 static gbblas_status_t gemv_n_narrow(gbblas_handle_t h, const GemvPolicy<T>& pol, int64_t m, int64_t n,
@@ -76,7 +76,7 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
   if (!tr) {
     gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
     if (try_rows_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;
-    if (m <= kNarrowRows) return gemv_n_narrow<T>(h, pol, m, n, a, lda, xb, incx, vec);
+    if (m <= narrow_rows<T>()) return gemv_n_narrow<T>(h, pol, m, n, a, lda, xb, incx, vec);
     SweepPlan p = plan_rows(m, n, h->sm_count, sizeof(T));
     T* partials = nullptr;
     if (p.split > 1) {
@@ -93,8 +93,9 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
           pol, m, n, a, lda, xb, incx, p.per_split, partials, h->tickets);
     return after_launch("gemv_n");
   }
-  if (m <= kNarrowRows) {
-    // at most kNarrowRows rows: one thread per column (cols_thread)
+  if (m <= kThreadRows) {
+    // at most kThreadRows rows: one thread per column (cols_thread; 8 x 2^22
+    // 25.6 us against 39.5 for cols_lanes)
     const int64_t grid = cdiv(n, kMvThreads);
     if (grid > INT32_MAX) return fail(GBBLAS_STATUS_UNSUPPORTED, "gemv: too many columns");
     if (vec)
@@ -103,6 +104,23 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
     else
       cols_thread<GemvPolicy<T>, T, false, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, int(m), n, a,
                                                                                                 lda, xb, incx);
+    return after_launch("gemv_t_narrow");
+  }
+  if (m <= narrow_rows<T>()) {
+    // up to 32 lanes x 16 bytes of rows: a few lanes per column (cols_lanes;
+    // 64 x 2^20 186 -> 65 us against a warp per column), up to 8 CTAs per SM
+    constexpr int RPT = 16 / sizeof(T);
+    int lpc_log2 = 0;
+    while ((int64_t(1) << lpc_log2) * RPT < m) ++lpc_log2;
+    const int64_t per_cta = int64_t(32 >> lpc_log2) * kMvWarps;
+    int64_t grid = cdiv(n, per_cta);
+    if (grid > 8 * int64_t(h->sm_count)) grid = 8 * int64_t(h->sm_count);
+    if (vec)
+      cols_lanes<GemvPolicy<T>, T, true, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, int(m), n, a, lda,
+                                                                                              xb, incx, lpc_log2);
+    else
+      cols_lanes<GemvPolicy<T>, T, false, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, int(m), n, a,
+                                                                                               lda, xb, incx, lpc_log2);
     return after_launch("gemv_t_narrow");
   }
   {

@@ -318,9 +318,14 @@ __global__ void __launch_bounds__(kMvThreads, 4)
 // ran at 356 GB/s.  Here a column takes `lpc` lanes (rows / RPT rounded up to
 // a power of two) and a warp covers 32 / lpc columns per load: a packed A
 // (lda == rows) streams in contiguous 512-byte warp loads.
-constexpr int kNarrowRows = 32;
+constexpr int kNarrowRows = 128;  // FP32 (32 lanes x 4 rows); FP64: 64
+template <typename T>
+constexpr int narrow_rows() {
+  return 32 * (16 / int(sizeof(T)));
+}
+constexpr int kThreadRows = 32;  // GEMV 't': one thread per column up to here, cols_lanes above
 
-// out(i) = fold over j of pol.add(A[i + j*lda], x[j]), i < M <= kNarrowRows.
+// out(i) = fold over j of pol.add(A[i + j*lda], x[j]), i < M <= narrow_rows<T>().
 // CTA b takes columns [b*cols_per_cta, ...); lanes with the same row group
 // are folded by shuffles, warps in warp order in shared memory, and the
 // CTAs' per-row partials by the last CTA to finish, all 256 threads over
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(kMvThreads)
                 unsigned int* __restrict__ tickets) {
   using Acc = typename P::Acc;
   constexpr int RPT = Pack16<T>::n;
-  __shared__ Acc red[kMvThreads];  // [warp][32 rows], later [run][row]
+  __shared__ Acc red[kMvWarps * kNarrowRows];  // [warp][row], later [run][row]
   __shared__ bool is_last;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int lpc = 1 << lpc_log2, cpw = 32 >> lpc_log2;
@@ -381,13 +386,13 @@ __global__ void __launch_bounds__(kMvThreads)
     for (int r = 0; r < RPT; ++r) pol.merge(acc[r], pol.shfl_down(acc[r], off));
   if (lane < lpc)
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) red[warp * 32 + r0 + r] = acc[r];
+    for (int r = 0; r < RPT; ++r) red[warp * kNarrowRows + r0 + r] = acc[r];
   __syncthreads();
   const int t = threadIdx.x;
   Acc s;
   if (t < M) {
     s = red[t];
-    for (int w = 1; w < kMvWarps; ++w) pol.merge(s, red[w * 32 + t]);
+    for (int w = 1; w < kMvWarps; ++w) pol.merge(s, red[w * kNarrowRows + t]);
   }
   if (gridDim.x == 1) {
     if (t < M) pol.finish(s, t);
@@ -418,7 +423,7 @@ __global__ void __launch_bounds__(kMvThreads)
   if (t == 0) tickets[0] = 0u;
 }
 
-// out(j) = fold over i < M of pol.add(A[i + j*lda], x[i]), M <= kNarrowRows:
+// out(j) = fold over i < M of pol.add(A[i + j*lda], x[i]), M <= kThreadRows (32):
 // one thread per column, its M values in at most 8 (FP32) 16-byte loads; x
 // in shared memory.  A packed A streams as contiguous 1 KB warp loads (8 x
 // 2^22 GEMV 't' ran at 221 GB/s with a warp per column).
@@ -428,7 +433,7 @@ __global__ void __launch_bounds__(kMvThreads)
                 int64_t incx) {
   using Acc = typename P::Acc;
   constexpr int RPT = Pack16<T>::n;
-  __shared__ T xs[kNarrowRows];
+  __shared__ T xs[kThreadRows];
   if (threadIdx.x < M) xs[threadIdx.x] = HAS_X ? xb[int64_t(threadIdx.x) * incx] : T(1);
   __syncthreads();
   const int64_t j = int64_t(blockIdx.x) * kMvThreads + threadIdx.x;
@@ -448,6 +453,57 @@ __global__ void __launch_bounds__(kMvThreads)
     for (int i = 0; i < M; ++i) pol.add(acc, col[i], xs[i]);
   }
   pol.finish(acc, j);
+}
+
+// out(j) = fold over i < M of pol.add(A[i + j*lda], x[i]), kThreadRows < M <= narrow_rows<T>():
+// a column takes `lpc` lanes as in rows_narrow, each lane one 16-byte group
+// of its rows (x of those rows held in registers), folded by shuffles in a
+// fixed tree; a warp covers 32 / lpc columns per load, so a packed A streams
+// in contiguous 512-byte warp loads (8 x 2^22 GEMV 't' ran at 221 GB/s with
+// a warp per column).  Grid-stride over columns, warp-uniform, so that every
+// lane takes part in the shuffles.
+template <class P, typename T, bool VEC, bool HAS_X>
+__global__ void __launch_bounds__(kMvThreads)
+    cols_lanes(P pol, int M, int64_t N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
+               int64_t incx, int lpc_log2) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lpc = 1 << lpc_log2, cpw = 32 >> lpc_log2;
+  const int sub = lane & (lpc - 1), r0 = sub * RPT;
+  T xr[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) xr[r] = r0 + r < M ? (HAS_X ? xb[int64_t(r0 + r) * incx] : T(1)) : T(0);
+  const bool full = VEC && r0 + RPT <= M;
+  const int64_t step = int64_t(cpw) * kMvWarps * gridDim.x;
+  constexpr int U = 4;
+  for (int64_t base = (int64_t(blockIdx.x) * kMvWarps + warp) * cpw; base < N; base += U * step) {
+    Acc acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      // columns past N read column N - 1 (in bounds, unconditional, so the U
+      // loads issue together) and are not stored
+      int64_t j = base + u * step + (lane >> lpc_log2);
+      if (j >= N) j = N - 1;
+      const T* col = A + j * lda + r0;
+      T v[RPT];
+      if (full) {
+        Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(col)), v);
+      } else {
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) v[r] = r0 + r < M ? col[r] : T(0);
+      }
+      acc[u] = pol.init();
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) pol.add(acc[u], v[r], xr[r]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      for (int off = lpc >> 1; off > 0; off >>= 1) pol.merge(acc[u], pol.shfl_down(acc[u], off));
+      const int64_t j = base + u * step + (lane >> lpc_log2);
+      if (sub == 0 && j < N) pol.finish(acc[u], j);
+    }
+  }
 }
 
 // ------------------------------------------------------------- cols sweep --

@@ -157,13 +157,17 @@ def test_gemv_t_warp_per_column_misaligned(sb, torch_cuda, m, n, lda, off):
 @pytest.mark.parametrize("trans", ["n", "t"])
 @pytest.mark.parametrize("m,n,lda,incx,incy", [(8, 1 << 22, 8, 1, 1), (3, 70001, 3, 1, 1), (32, 20000, 32, 2, 3),
                                                (17, 5003, 20, -1, 2), (1, 9000, 1, 1, 1), (5, 64, 7, 3, 1),
-                                               (32, 1, 32, 1, 1), (12, 0, 12, 1, 1)])
+                                               (32, 1, 32, 1, 1), (12, 0, 12, 1, 1), (64, 1 << 18, 64, 1, 1),
+                                               (33, 9001, 36, 1, 2), (48, 3000, 49, -2, 1), (100, 20001, 100, 1, 1),
+                                               (128, 3001, 130, 1, 3), (65, 777, 65, -1, 1)])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_gemv_narrow_rows(sb, torch_cuda, trans, m, n, lda, incx, incy, dtype):
-    """At most 32 rows: 'n' runs rows_narrow (several columns per warp load,
-    the CTAs' partials folded by the last CTA), 't' runs cols_thread (one
-    thread per column); packed, padded and odd leading dimensions, strided
-    and reversed x, strided y, no columns at all."""
+    """Short, wide A (up to 128 FP32 / 64 FP64 rows; FP64 rows beyond take
+    the general sweeps): 'n' runs rows_narrow (several columns per warp load,
+    the CTAs' partials folded by the last CTA), 't' cols_thread (up to 32
+    rows) or cols_lanes (a few lanes per column, shuffle-folded); packed,
+    padded and odd leading dimensions, strided and reversed x, strided y, no
+    columns at all."""
     torch = torch_cuda
     from portblas_gb300 import blas
     g = rng(m + n + lda + int(dtype == np.float64))
