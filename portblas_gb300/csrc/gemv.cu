@@ -77,6 +77,18 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
     gbblas_status_t st = GBBLAS_STATUS_SUCCESS;
     if (try_rows_sweep_tma<GemvPolicy<T>, T, true>(h, pol, m, n, a, lda, xb, incx, &st)) return st;
     if (m <= narrow_rows<T>()) return gemv_n_narrow<T>(h, pol, m, n, a, lda, xb, incx, vec);
+    if (n <= kTallCols && m >= 64 * int64_t(h->sm_count)) {
+      // tall, narrow A: a warp per 32 x RPT rows over every column (rows_tall)
+      const int64_t grid = cdiv(m, int64_t(kMvThreads) * (16 / sizeof(T)));
+      if (grid > INT32_MAX) return fail(GBBLAS_STATUS_UNSUPPORTED, "gemv: too many rows");
+      if (vec)
+        rows_tall<GemvPolicy<T>, T, true, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, m, int(n), a, lda,
+                                                                                               xb, incx);
+      else
+        rows_tall<GemvPolicy<T>, T, false, true><<<unsigned(grid), kMvThreads, 0, h->stream>>>(pol, m, int(n), a,
+                                                                                                lda, xb, incx);
+      return after_launch("gemv_n_tall");
+    }
     SweepPlan p = plan_rows(m, n, h->sm_count, sizeof(T));
     T* partials = nullptr;
     if (p.split > 1) {

@@ -506,6 +506,69 @@ __global__ void __launch_bounds__(kMvThreads)
   }
 }
 
+// out(i) = fold over j < N of pol.add(A[i + j*lda], x[j]) for tall, narrow A
+// (N <= kTallCols): a warp owns 32 x RPT rows over every column, so a lane
+// keeps N loads of its rows in flight and no partial sums cross warps (the
+// rows sweep gave each warp one column of 128 rows: 4M x 8 GEMV 'n' at
+// 2207 GB/s).
+constexpr int kTallCols = 32;
+
+template <class P, typename T, bool VEC, bool HAS_X>
+__global__ void __launch_bounds__(kMvThreads)
+    rows_tall(P pol, int64_t M, int N, const T* __restrict__ A, int64_t lda, const T* __restrict__ xb,
+              int64_t incx) {
+  using Acc = typename P::Acc;
+  constexpr int RPT = Pack16<T>::n;
+  constexpr int WR = 32 * RPT;
+  __shared__ T xs[kTallCols];
+  if (threadIdx.x < N) xs[threadIdx.x] = HAS_X ? xb[int64_t(threadIdx.x) * incx] : T(1);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rb = (int64_t(blockIdx.x) * kMvWarps + warp) * WR;
+  if (rb >= M) return;
+  // offset (within the warp's rows) of the r-th row this lane owns
+  auto rof = [&](int r) { return VEC ? lane * RPT + r : r * 32 + lane; };
+  const bool full = VEC && rb + rof(0) + RPT <= M;
+  const T* Ab = A + rb;
+  Acc acc[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) acc[r] = pol.init();
+  constexpr int U = 8;
+  int j = 0;
+  for (; j + U <= N; j += U) {
+    T v[U][RPT];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const T* col = Ab + int64_t(j + u) * lda;
+      if (full) {
+        Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(col + rof(0))), v[u]);
+      } else {
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) v[u][r] = rb + rof(r) < M ? col[rof(r)] : T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[u][r], xs[j + u]);
+  }
+  for (; j < N; ++j) {
+    const T* col = Ab + int64_t(j) * lda;
+    T v[RPT];
+    if (full) {
+      Pack16<T>::get(__ldcs(reinterpret_cast<const typename Pack16<T>::V*>(col + rof(0))), v);
+    } else {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) v[r] = rb + rof(r) < M ? col[rof(r)] : T(0);
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) pol.add(acc[r], v[r], xs[j]);
+  }
+#pragma unroll
+  for (int r = 0; r < RPT; ++r)
+    if (rb + rof(r) < M) pol.finish(acc[r], rb + rof(r));
+}
+
 // ------------------------------------------------------------- cols sweep --
 // CTA = 8 warps over CC columns and one chunk of `rows_per_split` rows; x of
 // the chunk is staged in shared memory; warp w takes columns w, w+8, ... and

@@ -192,3 +192,35 @@ def test_gemv_narrow_rows(sb, torch_cuda, trans, m, n, lda, incx, incy, dtype):
     mask[: ylen * incy: incy] = False
     np.testing.assert_array_equal(out[mask], y[mask])
     sb.check_device_error()
+
+
+@pytest.mark.parametrize("trans", ["n", "t"])
+@pytest.mark.parametrize("m,n,lda,incx,incy", [(20000, 8, 20000, 1, 1), (50001, 3, 50004, -1, 2),
+                                               (30000, 32, 30001, 2, 1), (1 << 20, 17, 1 << 20, 1, 3)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_gemv_tall_narrow(sb, torch_cuda, trans, m, n, lda, incx, incy, dtype):
+    """Tall, narrow A (at most 32 columns, rows beyond 64 per SM): 'n' runs
+    rows_tall (a warp per 32 x RPT rows over every column); aligned and
+    unaligned leading dimensions, ragged last rows, strided and reversed x,
+    strided y; against the FP64 oracle, |A||x|-normalised."""
+    torch = torch_cuda
+    from portblas_gb300 import blas
+    g = rng(m + n + lda + int(dtype == np.float64))
+    a = g.uniform(-1, 1, lda * n).astype(dtype)
+    xlen, ylen = (n, m) if trans == "n" else (m, n)
+    x = g.uniform(-1, 1, xlen * abs(incx)).astype(dtype)
+    y = g.uniform(-1, 1, ylen * incy).astype(dtype)
+    ref = oracle.gemv(trans, m, n, 0.75, a, lda, x, incx, 0.5, y, incy)
+    yd = to_dev(y, torch)
+    blas._gemv(sb, trans, m, n, 0.75, to_dev(a, torch), lda, to_dev(x, torch), incx, 0.5, yd, incy)
+    out = to_host(yd)
+    got = oracle.view(out, ylen, incy)
+    A2 = a.reshape(n, lda)[:, :m].astype(np.float64).T
+    xv = np.abs(oracle.view(x, xlen, incx).astype(np.float64))
+    scale = 0.75 * (np.abs(A2) @ xv if trans == "n" else np.abs(A2).T @ xv)
+    scale = scale + 0.5 * np.abs(oracle.view(y, ylen, incy).astype(np.float64))
+    assert (np.abs(got - ref) / scale).max() <= 256 * np.finfo(dtype).eps
+    mask = np.ones(len(y), bool)
+    mask[: ylen * incy: incy] = False
+    np.testing.assert_array_equal(out[mask], y[mask])
+    sb.check_device_error()
