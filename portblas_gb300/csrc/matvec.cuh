@@ -640,11 +640,28 @@ __global__ void __launch_bounds__(kMvThreads, 8)
   __syncthreads();
   if (!is_last) return;
   __threadfence();
+  // every thread folds a run of the splits for one column, then the runs are
+  // folded in order (a long, narrow A has over a thousand splits; folded by
+  // one thread per column they dominated 4M x 8 GEMV 't')
+  __shared__ Acc runsum[kMvThreads];
+  const int runs = kMvThreads / cols_per_cta;
+  const int64_t nsp = gridDim.y, per = (nsp + runs - 1) / runs;
+  {
+    const int cc = threadIdx.x % cols_per_cta, run = threadIdx.x / cols_per_cta;
+    if (run < runs) {
+      Acc f = pol.init();
+      const int64_t s1 = min(nsp, (run + 1) * per);
+      if (cbase + cc < N)
+        for (int64_t sp = run * per; sp < s1; ++sp) pol.merge(f, ldcg_any(partials + sp * N + cbase + cc));
+      runsum[run * cols_per_cta + cc] = f;
+    }
+  }
+  __syncthreads();
   for (int cc = threadIdx.x; cc < cols_per_cta; cc += blockDim.x) {
     const int64_t jcol = cbase + cc;
     if (jcol >= N) break;
-    Acc f = ldcg_any(partials + jcol);
-    for (unsigned sp = 1; sp < gridDim.y; ++sp) pol.merge(f, ldcg_any(partials + int64_t(sp) * N + jcol));
+    Acc f = runsum[cc];
+    for (int run = 1; run < runs; ++run) pol.merge(f, runsum[run * cols_per_cta + cc]);
     pol.finish(f, jcol);
   }
   if (threadIdx.x == 0) tickets[blockIdx.x] = 0u;
