@@ -22,7 +22,10 @@ def test_learned_selector_beats_heuristic(sb, torch_cuda, dtype, count, seed):
     code = sweep.DTYPE_F64 if dtype == "f64" else sweep.DTYPE_F32
     r_mlp, r_heur = [], []
     for s in sweep.sample_shapes(count, seed=seed, dtype=dtype):
-        t = R.time_all(s, e0, e1, min_ms=0.1, max_reps=5)
+        # the faster of two timing passes per config, so that a one-off stall
+        # in one pass is not read as regret (one pass once showed a 130%
+        # outlier on a single shape)
+        t = np.minimum(R.time_all(s, e0, e1, min_ms=0.1, max_reps=5), R.time_all(s, e0, e1, min_ms=0.1, max_reps=5))
         pick = C.c_int()
         assert L.gbblas_gemm_selector_pick(code, s["m"], s["n"], s["k"], b"t" if s["ta"] else b"n",
                                            b"t" if s["tb"] else b"n", s["lda"], s["ldb"], s["ldc"], s["batch"],
