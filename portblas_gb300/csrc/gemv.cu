@@ -7,6 +7,10 @@
 // each output tile; the alpha/beta epilogue is fused.  beta == 0 never reads
 // y (blas2_interface.hpp:205-211); trans 'n'/'N' is the normal sweep and any
 // other character the transposed one (blas2_interface.hpp:1163-1192).
+// Short, wide A (at most 32 lanes x 16 bytes of rows) and, for 'n', tall A
+// of at most 32 columns take kernels shaped for them (matvec.cuh:
+// rows_narrow, cols_thread, cols_lanes, rows_tall), so that every warp load
+// stays a contiguous run of the matrix.
 #include "stream_sweep.cuh"
 
 namespace gb {
@@ -121,7 +125,6 @@ gbblas_status_t gemv_impl(gbblas_handle_t h, char trans, int64_t m, int64_t n, T
   if (m <= narrow_rows<T>()) {
     // up to 32 lanes x 16 bytes of rows: a few lanes per column (cols_lanes;
     // 64 x 2^20 186 -> 65 us against a warp per column), up to 8 CTAs per SM
-    constexpr int RPT = 16 / sizeof(T);
     int lpc_log2 = 0;
     while ((int64_t(1) << lpc_log2) * RPT < m) ++lpc_log2;
     const int64_t per_cta = int64_t(32 >> lpc_log2) * kMvWarps;
